@@ -1,0 +1,141 @@
+/*
+ * qca_gb300 — C ABI of the GB300 (sm_103a) time-evolution library for the
+ * quantum game of life of BenjaminDecker/quantum-cellular-automaton.
+ *
+ * Every entry point returns an int status (QCA_OK = 0); the message of the last
+ * failure on the calling host thread is returned by qca_last_error().  No entry
+ * point traps on the device; numerical failures come back as status codes.
+ * Host arrays are plain C arrays; complex numbers are interleaved (re, im)
+ * doubles, i.e. the memory layout of numpy complex128 in C order.  `stream` is a
+ * cudaStream_t passed as void* (NULL = the legacy default stream).  A handle may
+ * be used by one host thread at a time; calls on it are stream ordered.
+ *
+ * The reference interfaces each entry point replaces are cited as
+ * file:line of the reference project.
+ */
+#ifndef QCA_GB300_H
+#define QCA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------- */
+#define QCA_OK 0
+#define QCA_ERR_INVALID 1        /* bad argument (reference: assert / ValueError)      */
+#define QCA_ERR_CUDA 2           /* CUDA runtime error                                  */
+#define QCA_ERR_OOM 3            /* device allocation failed                            */
+#define QCA_ERR_BREAKDOWN 4      /* Krylov breakdown that could not be absorbed         */
+#define QCA_ERR_NOT_CONVERGED 5  /* Lanczos / Jacobi iteration limit reached            */
+#define QCA_ERR_NAN 6            /* non-finite norm detected                            */
+#define QCA_ERR_ADMISSION 7      /* device-memory budget would be exceeded              */
+#define QCA_ERR_NO_DEVICE 8      /* no CUDA device / sm_103a image not loadable         */
+
+/* ---- precision ------------------------------------------------------------- */
+#define QCA_PREC_FP64 0  /* complex128 storage and arithmetic ("plain")                 */
+#define QCA_PREC_MIXED 1 /* complex64 storage, fp32 products, fp64 Krylov scalars, SVD
+                            singular values, truncation weights and normalisation       */
+
+/* ---- algorithms (parameters/parser.py:75-82) -------------------------------- */
+#define QCA_ALGO_1TDVP 1
+#define QCA_ALGO_2TDVP 2
+
+const char* qca_last_error(void);
+int qca_version(void);
+/* Number of CUDA devices the library can run on (0 when none). */
+int qca_device_count(int* count);
+
+/* =============================================================================
+ * Exact state-vector evolution.
+ * Replaces algorithms/exact.py:9-28 (Exact.__init__, Exact.do_time_step,
+ * the psi property) and the dense propagator lautils/lautils.py:44-54.
+ * The Hamiltonian H = sum_i X_i Pi_i of parameters/rules.py is applied matrix
+ * free: cell i flips iff the number of alive cells j != i with |i-j| <= distance
+ * lies in [interval_lo, interval_hi) (upper bound excluded, as the Python range
+ * of parameters/parser.py:182).  Cell 0 is the most significant bit of the
+ * amplitude index (tensor_networks/mps.py:194-208).  One step applies
+ * exp(-i pi/2 step_size H) by Lanczos with `krylov_dim` vectors resident on the
+ * device, split into sub-steps when step_size * ||H|| is large.
+ * ============================================================================= */
+typedef struct qca_exact qca_exact;
+
+/* Exact.__init__ (exact.py:15-17).  precision: QCA_PREC_FP64 or QCA_PREC_MIXED. */
+int qca_exact_create(int n_cells, int distance, int interval_lo, int interval_hi, int precision,
+                     int krylov_dim, qca_exact** out);
+int qca_exact_destroy(qca_exact* h);
+/* psi setter (exact.py:23-25): 2^n complex128 amplitudes from HOST memory. */
+int qca_exact_set_state(qca_exact* h, const double* psi, void* stream);
+/* psi setter from DEVICE memory (complex128 for FP64, complex64 for MIXED). */
+int qca_exact_set_state_device(qca_exact* h, const void* psi_dev, void* stream);
+/* psi getter (exact.py:19-21): 2^n complex128 amplitudes into HOST memory. */
+int qca_exact_get_state(qca_exact* h, double* psi, void* stream);
+/* Device pointer of the resident state (complex128 or complex64 by precision). */
+int qca_exact_state_device(qca_exact* h, void** psi_dev);
+/* do_time_step (exact.py:27-28) repeated nsteps times with step size dt. */
+int qca_exact_step(qca_exact* h, double step_size, int nsteps, void* stream);
+/* <n_i> and the 2x2 single-site density matrices rho_i (4 complex128 per cell,
+ * row major) of the current state; either output may be NULL.  The reference
+ * measures through MPS.from_vector (mps.py:54-73) and MPS.measure (mps.py:100-140). */
+int qca_exact_measure(qca_exact* h, double* population, double* rho, void* stream);
+/* Bytes of device memory the handle holds. */
+int qca_exact_footprint(int n_cells, int precision, int krylov_dim, size_t* bytes);
+
+/* =============================================================================
+ * TDVP engine: many MPS chains evolved side by side on one device.
+ * Replaces algorithms/tdvp.py:10-365 (TDVP.__init__, do_time_step, the 1-site
+ * and 2-site sweeps, _evolve_split_and_truncate, _evolve_site, _evolve_bond,
+ * the environment updates) with the local exponential of lautils.py:57-81
+ * computed by Lanczos, and MPS.measure (mps.py:100-140).
+ * ============================================================================= */
+typedef struct qca_engine qca_engine;
+
+typedef struct qca_chain_desc {
+  int n_sites;             /* N >= 2                                                   */
+  const int* mpo_bonds;    /* N+1 MPO bond dimensions w_0..w_N (w_0 = w_N = 1)           */
+  const double* mpo;       /* W[0..N-1] concatenated; W[i] is (2,2,w_i,w_{i+1}) complex128
+                              in C order (tensor_networks/mpo.py:158-200)               */
+  const int* mps_bonds;    /* N+1 MPS bond dimensions D_0..D_N (D_0 = D_N = 1)           */
+  const double* mps;       /* A[0..N-1] concatenated; A[i] is (2,D_i,D_{i+1}) complex128
+                              (tensor_networks/mps.py:14-25)                            */
+  int algorithm;           /* QCA_ALGO_1TDVP or QCA_ALGO_2TDVP (tdvp.py:55-63)           */
+  int max_bond_dim;        /* --max-bond-dim (parameters/parser.py:106-113)             */
+  double svd_epsilon;      /* --svd-epsilon (parameters/parser.py:114-122)              */
+  double step_size;        /* dt; the local propagator is exp(-i pi/2 dt/2 H_eff)        */
+} qca_chain_desc;
+
+/* Create an engine on the current device.  hbm_budget_bytes bounds the device memory
+ * all its chains may hold (0 = 90% of the free memory at creation). */
+int qca_engine_create(int precision, size_t hbm_budget_bytes, qca_engine** out);
+int qca_engine_destroy(qca_engine* e);
+/* Device bytes a chain of this description would hold (admission estimate). */
+int qca_chain_footprint(const qca_chain_desc* d, int precision, size_t* bytes);
+/* TDVP.__init__ (tdvp.py:12-40): upload, canonicalise, build right environments.
+ * Returns QCA_ERR_ADMISSION when the budget would be exceeded. */
+int qca_chain_add(qca_engine* e, const qca_chain_desc* d, void* stream, int* chain_id);
+int qca_chain_remove(qca_engine* e, int chain_id);
+/* TDVP.do_time_step (tdvp.py:50-63) nsteps times for every chain of the engine. */
+int qca_engine_step(qca_engine* e, int nsteps, void* stream);
+/* do_time_step nsteps times for the listed chains only (the others keep their state). */
+int qca_engine_step_chains(qca_engine* e, const int* chain_ids, int count, int nsteps, void* stream);
+/* Algorithm.measure (algorithm.py:58-63 -> mps.py:100-140).  Mutates the gauge of the
+ * stored MPS exactly like the reference.  Outputs: population[N], d_population[N],
+ * single_site_entropy[N], bond_dims[N+1] (any may be NULL). */
+int qca_chain_measure(qca_engine* e, int chain_id, double* population, double* d_population,
+                      double* single_site_entropy, double* bond_dims, void* stream);
+/* Current MPS bond dimensions D_0..D_N. */
+int qca_chain_bonds(qca_engine* e, int chain_id, int* bonds);
+/* psi getter (tdvp.py:42-44): the MPS tensors into host memory, concatenated like
+ * qca_chain_desc.mps; `capacity` is the number of doubles available. */
+int qca_chain_get_mps(qca_engine* e, int chain_id, double* mps, size_t capacity, void* stream);
+/* Statistics of the last step of a chain: [0] largest Lanczos dimension used,
+ * [1] summed discarded weight (sum of squared truncated singular values). */
+int qca_chain_stats(qca_engine* e, int chain_id, double* stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QCA_GB300_H */

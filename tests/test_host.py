@@ -1,0 +1,101 @@
+"""Host-side logic that needs no GPU: the product's MPO / MPS builders against the
+reference fixtures, and the C-ABI library's exported symbols."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import qca_gb300
+from qca_gb300 import _lib
+from qca_gb300.tensor_networks import MPO, MPS, Rules, rule_from_mpo
+
+from conftest import ROOT
+
+RULES = [(1, 1, 2), (1, 2, 4), (1, 2, 5), (2, 1, 2), (2, 2, 4), (2, 2, 5), (3, 1, 2), (3, 2, 4), (3, 2, 5)]
+
+
+@pytest.mark.parametrize("d,lo,hi", RULES)
+def test_mpo_builder_matches_reference(golden, d, lo, hi):
+    g = golden("mpo_rules.npz")
+    W = MPO.hamiltonian_from_rules(Rules(6, range(lo, hi), d)).W
+    key = f"d{d}_{lo}{hi}"
+    assert np.array_equal(W[2], g[key + "_bulk"])
+    assert np.array_equal(W[0], g[key + "_first"])
+    assert np.array_equal(W[-1], g[key + "_last"])
+
+
+@pytest.mark.parametrize("d,lo,hi", RULES)
+def test_rule_recovered_from_plain_w_list(golden, d, lo, hi):
+    g = golden("mpo_rules.npz")
+    key = f"d{d}_{lo}{hi}"
+
+    class Bare:  # what the reference's MPO exposes: only W
+        W = [g[key + "_first"]] + [g[key + "_bulk"]] * 4 + [g[key + "_last"]]
+
+    dist, interval = rule_from_mpo(Bare)
+    # equivalent rules (e.g. [2,4) and [2,5) at distance 1) give the same H
+    from oracle import qca_oracle as O
+    a = O.sparse_rule_hamiltonian(7, dist, interval).toarray()
+    b = O.sparse_rule_hamiltonian(7, d, range(lo, hi)).toarray()
+    assert np.array_equal(a, b)
+
+
+def test_mps_constructors_match_reference(golden):
+    m = golden("measure_case.npz")
+    A = MPS.from_vector(m["psi"])
+    assert np.array_equal(np.array([a.shape for a in A.A]), m["from_vector_shapes"])
+    assert np.abs(A.as_vector() - m["as_vector"]).max() < 1e-14
+    p = m["prod_p"]
+    v = MPS.from_density_distribution(p).as_vector()
+    assert abs(np.linalg.norm(v) - 1.0) < 1e-14
+
+
+def test_mps_npz_roundtrip(tmp_path):
+    A = MPS.from_vector(np.random.default_rng(1).standard_normal(32) + 0j)
+    path = tmp_path / "s.npz"
+    A.write_to_file(str(path))
+    B = MPS.from_file(str(path))
+    for a, b in zip(A.A, B.A):
+        assert np.array_equal(a, b)
+
+
+def test_classical_evolution_blinker():
+    from qca_gb300.algorithms import Algorithm
+    rules = Rules(5, range(1, 2), 1)
+    first = np.array([0.0, 0.0, 1.0, 0.0, 0.0])
+    heat = Algorithm.classical_evolution(first, rules, 3)
+    assert heat.shape == (3, 5)
+    assert np.array_equal(heat[1], [0.0, 1.0, 1.0, 1.0, 0.0])
+
+
+def _header_functions():
+    src = open(os.path.join(ROOT, "include", "qca_gb300.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(qca_\w+)\s*\(", src, re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _lib.load()
+    names = _header_functions()
+    assert len(names) >= 20
+    for name in names:
+        assert hasattr(lib, name), name
+    assert set(_lib.SIGNATURES) | {"qca_last_error", "qca_version"} == set(names)
+
+
+def test_library_reports_errors_without_a_gpu():
+    lib = _lib.load()
+    out = ctypes.c_void_p()
+    # invalid arguments are rejected before any device call
+    st = lib.qca_exact_create(1, 1, 1, 2, 0, 30, ctypes.byref(out))
+    assert st == _lib.QCA_ERR_INVALID
+    assert b"invalid" in lib.qca_last_error()
+    with pytest.raises(_lib.QcaError):
+        _lib.check(st)
+
+
+def test_footprint_estimates():
+    size = ctypes.c_size_t()
+    _lib.call("qca_exact_footprint", 24, _lib.QCA_PREC_FP64, 30, ctypes.byref(size))
+    assert size.value >= 30 * 16 * (1 << 24)

@@ -1,0 +1,89 @@
+"""The oracle against the reference's own outputs (golden fixtures made by
+tests/golden/make_golden.py from the reference implementation)."""
+import numpy as np
+import pytest
+
+from oracle import qca_oracle as O
+
+RULES = [(1, 1, 2), (1, 2, 4), (1, 2, 5), (2, 1, 2), (2, 2, 4), (2, 2, 5), (3, 1, 2), (3, 2, 4), (3, 2, 5)]
+
+
+@pytest.mark.parametrize("d,lo,hi", RULES)
+def test_oracle_mpo_matches_reference(golden, d, lo, hi):
+    g = golden("mpo_rules.npz")
+    W = O.build_mpo(O.Rules(6, range(lo, hi), d))
+    key = f"d{d}_{lo}{hi}"
+    assert np.array_equal(W[2], g[key + "_bulk"])
+    assert np.array_equal(W[0], g[key + "_first"])
+    assert np.array_equal(W[-1], g[key + "_last"])
+
+
+@pytest.mark.parametrize("d,lo,hi", RULES)
+def test_oracle_matrix_free_equals_mpo(d, lo, hi):
+    n = 7
+    Hm = O.mpo_as_matrix(O.build_mpo(O.Rules(n, range(lo, hi), d)))
+    Hs = O.sparse_rule_hamiltonian(n, d, range(lo, hi)).toarray()
+    assert np.abs(Hm - Hs).max() == 0.0
+    assert np.abs(Hs - Hs.T).max() == 0.0
+
+
+@pytest.mark.parametrize("name", ["single8", "rand10"])
+def test_oracle_exact_matches_reference(golden, name):
+    e = golden("exact_series.npz")
+    n, d, lo, hi, dt, steps = e[name + "_meta"]
+    n, d, steps = int(n), int(d), int(steps)
+    psi = O.product_state_vector(e[name + "_p"])
+    for s in range(steps + 1):
+        pop = O.populations_from_vector(psi, n)
+        assert np.abs(pop - e[name + "_pop"][s]).max() < 1e-12
+        psi = O.exact_evolve(psi, n, d, range(int(lo), int(hi)), float(dt), 1)
+
+
+CASES = ["t2_single8", "t1_single8", "t2_rand7", "t1_rand7", "t2_rand9_d3"]
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("mode", ["fixed", "ref"])
+def test_oracle_tdvp_matches_reference(golden, name, mode):
+    t = golden("tdvp_series.npz")
+    n, d, lo, hi, dt, chi, eps, steps = t[name + "_meta"]
+    n, d, steps = int(n), int(d), int(steps)
+    W = O.build_mpo(O.Rules(n, range(int(lo), int(hi)), d))
+    orc = O.TDVPOracle(O.mps_from_density_distribution(t[name + "_p"]), W, str(t[name + "_alg"]), float(dt),
+                       int(chi), float(eps), fixed=(mode == "fixed"))
+    for s in range(steps + 1):
+        pop, dpop, sse, bonds = orc.measure()
+        assert np.abs(pop - t[f"{name}_{mode}_pop"][s]).max() < 1e-12
+        assert np.array_equal(bonds, t[f"{name}_{mode}_bonds"][s])
+        assert np.nanmax(np.abs(sse - t[f"{name}_{mode}_sse"][s])) < 1e-10
+        if s < steps:
+            orc.step()
+
+
+def test_oracle_measure_matches_reference(golden):
+    m = golden("measure_case.npz")
+    pop, dpop, sse, b = O.measure(O.mps_from_vector(m["psi"]))
+    assert np.abs(pop - m["pop"]).max() < 1e-14
+    assert np.abs(sse - m["sse"]).max() < 1e-12
+    assert np.array_equal(b, m["bonds"])
+    A = O.mps_from_vector(m["psi"])
+    assert np.array_equal(np.array([a.shape for a in A]), m["from_vector_shapes"])
+    assert np.abs(O.mps_as_vector(A) - m["as_vector"]).max() < 1e-14
+
+
+def test_oracle_qr_convention(golden):
+    """numpy.linalg.qr (the call at mps.py:86) as the convention the device QR follows."""
+    g = golden("qr_lapack.npz")
+    for k in range(5):
+        a = g[f"a{k}"]
+        for mode in ("reduced", "complete"):
+            q, r = np.linalg.qr(a, mode=mode)
+            assert np.abs(q - g[f"a{k}_{mode}_q"]).max() < 1e-13
+            assert np.abs(r - g[f"a{k}_{mode}_r"]).max() < 1e-13
+
+
+def test_truncation_rule():
+    s = np.array([1.0, 0.1, 1e-5, 1e-9, 1e-12])
+    assert O.truncation_rank(s, 10, 1e-8) == 3
+    assert O.truncation_rank(s, 2, 1e-8) == 2
+    assert O.truncation_rank(s, 10, 1e-13) == 5
