@@ -1,0 +1,109 @@
+"""TDVP on the GPU against the reference's own outputs (gauge-consistent form,
+golden fixtures from tests/golden/make_golden.py) and against the oracle.
+
+Tolerances (spec bounds): FP64 plain path max|d<n_i>| <= 1e-8 with
+identical truncated bond dimensions; mixed path max|d<n_i>| <= 1e-5."""
+import types
+
+import numpy as np
+import pytest
+
+from oracle import qca_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL_FP64 = 1e-8
+TOL_MIXED = 1e-5
+CASES = ["t2_single8", "t1_single8", "t2_rand7", "t1_rand7", "t2_rand9_d3"]
+
+
+def make(alg_name, n, d, lo, hi, p, dt, chi, eps, precision="fp64", engine=None):
+    from qca_gb300 import GpuTDVP, MPO, MPS, Rules
+    H = MPO.hamiltonian_from_rules(Rules(n, range(lo, hi), d))
+    args = types.SimpleNamespace(step_size=dt, algorithm=alg_name, max_bond_dim=chi, svd_epsilon=eps,
+                                 precision=precision)
+    return GpuTDVP(MPS.from_density_distribution(p), H, args, engine=engine)
+
+
+def rows(n):
+    return np.zeros(n), np.zeros(n), np.zeros(n), np.zeros(n + 1)
+
+
+def meta(t, name):
+    n, d, lo, hi, dt, chi, eps, steps = t[name + "_meta"]
+    return int(n), int(d), int(lo), int(hi), float(dt), int(chi), float(eps), int(steps)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_tdvp_fp64_matches_reference_fixed(golden, name):
+    t = golden("tdvp_series.npz")
+    n, d, lo, hi, dt, chi, eps, steps = meta(t, name)
+    alg = make(str(t[name + "_alg"]), n, d, lo, hi, t[name + "_p"], dt, chi, eps)
+    for s in range(steps + 1):
+        pop, dpop, sse, bonds = rows(n)
+        alg.measure(pop, dpop, sse, bonds)
+        assert np.abs(pop - t[f"{name}_fixed_pop"][s]).max() < TOL_FP64, s
+        assert np.array_equal(bonds, t[f"{name}_fixed_bonds"][s]), (s, bonds)
+        assert np.abs(sse - t[f"{name}_fixed_sse"][s]).max() < 1e-6
+        if s < steps:
+            alg.do_time_step()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_tdvp_mixed_matches_reference_fixed(golden, name):
+    t = golden("tdvp_series.npz")
+    n, d, lo, hi, dt, chi, eps, steps = meta(t, name)
+    alg = make(str(t[name + "_alg"]), n, d, lo, hi, t[name + "_p"], dt, chi, max(eps, 1e-6), "mixed")
+    for s in range(steps + 1):
+        pop, dpop, sse, bonds = rows(n)
+        alg.measure(pop, dpop, sse, bonds)
+        assert np.abs(pop - t[f"{name}_fixed_pop"][s]).max() < TOL_MIXED, s
+        if s < steps:
+            alg.do_time_step()
+
+
+@pytest.mark.parametrize("alg_name", ["2tdvp", "1tdvp"])
+def test_tdvp_state_matches_oracle_without_measurements(alg_name):
+    n, d, lo, hi, dt, chi, eps, steps = 9, 2, 2, 4, 0.05, 12, 1e-9, 4
+    p = np.sin(O.random_thetas(n, 77)) ** 2
+    alg = make(alg_name, n, d, lo, hi, p, dt, chi, eps)
+    W = O.build_mpo(O.Rules(n, range(lo, hi), d))
+    orc = O.TDVPOracle(O.mps_from_density_distribution(p), W, alg_name, dt, chi, eps, fixed=True)
+    alg.evolve(steps)
+    for _ in range(steps):
+        orc.step()
+    got = alg.psi.as_vector()
+    ref = O.mps_as_vector(orc.A)
+    assert np.abs(got - ref).max() < TOL_FP64
+    assert alg.bonds() == [a.shape[1] for a in orc.A] + [1]
+
+
+def test_tdvp_batched_equals_alone():
+    """Chains of different length, rule and bond cap stepped together in one engine
+    give the same populations as each chain stepped alone."""
+    from qca_gb300.algorithms import _Engine
+    from qca_gb300 import _lib
+    specs = [("2tdvp", 8, 1, 1, 2, 8), ("2tdvp", 11, 2, 2, 4, 16), ("1tdvp", 7, 2, 2, 4, 8), ("2tdvp", 6, 3, 2, 5, 8)]
+    eng = _Engine(_lib.QCA_PREC_FP64)
+    together = []
+    for k, (a, n, d, lo, hi, chi) in enumerate(specs):
+        p = np.sin(O.random_thetas(n, 100 + k)) ** 2
+        together.append(make(a, n, d, lo, hi, p, 0.05, chi, 1e-9, engine=eng))
+    import ctypes
+    ids = (ctypes.c_int * len(together))(*[g._chain for g in together])
+    _lib.call("qca_engine_step_chains", eng.h, ids, len(together), 3, None)
+    for k, (a, n, d, lo, hi, chi) in enumerate(specs):
+        p = np.sin(O.random_thetas(n, 100 + k)) ** 2
+        alone = make(a, n, d, lo, hi, p, 0.05, chi, 1e-9)
+        alone.evolve(3)
+        r1, r2 = rows(n), rows(n)
+        together[k].measure(*r1)
+        alone.measure(*r2)
+        assert np.abs(r1[0] - r2[0]).max() < 1e-12
+        assert np.array_equal(r1[3], r2[3])
+
+
+def test_tdvp_rejects_bad_arguments():
+    from qca_gb300 import _lib
+    with pytest.raises((ValueError, _lib.QcaError)):
+        make("2tdvp", 6, 1, 1, 2, np.zeros(6), 0.1, 0, 1e-8)
