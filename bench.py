@@ -1,0 +1,436 @@
+"""Benchmark of the GB300 time-evolution path: one JSON line on rank 0.
+
+Workloads (``--workload``):
+  batched (default)  256 independent 2TDVP chains in one engine, the batched
+                     configuration: N ~ U{16..96}, distance in {1,2,3},
+                     interval in {[1,1],[2,3],[2,4]}, bond cap in {32,64,128},
+                     random product states, dt = 0.05, mixed precision.
+                     One step = one TDVP time step of every chain.
+                     Metric: site-updates/s (2(N-1) per chain per step).
+  exact              2^24-amplitude exact evolution, distance 2, interval [2,3],
+                     Krylov dimension 30, dt = 0.05 (amplitude-updates/s).
+  single             single-chain 2TDVP, N = 64, distance 2, interval [2,3],
+                     bond cap 256, cutoff 1e-10, dt = 0.05, mixed precision.
+
+``--impl reference`` times the reference algorithm on the host cores instead:
+the oracle's NumPy restatement of tdvp.py (dense effective Hamiltonian +
+eigh, the reference's own cost profile) on a bounded sample of the same
+workload.  Under torchrun every rank runs its own independent chains (weak
+scaling, no data-path collective); only the timing uses a barrier and a max.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="batched", choices=["batched", "exact", "single"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--chains", type=int, default=256)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+# --------------------------------------------------------------------------- helpers
+class Dist:
+    def __init__(self, gpus: int):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def peaks() -> dict:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"],
+                "bf16_tflops_sustained": d.get("bf16_tflops_sustained", d["bf16_tflops"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "source": "fallback"}
+
+
+KCLASS = ["gemm", "mpo_apply", "lanczos_vec", "lanczos_exp", "svd", "qr", "other"]
+
+
+def kernel_stats(eng) -> dict:
+    from qca_gb300 import _lib
+    out = np.zeros(4 * len(KCLASS))
+    _lib.call("qca_engine_kernel_stats", eng.h, out.ctypes.data_as(_lib._PD), 1)
+    return {KCLASS[c]: {"launches": out[4 * c], "ms": out[4 * c + 1], "flops": out[4 * c + 2],
+                        "bytes": out[4 * c + 3]} for c in range(len(KCLASS))}
+
+
+def cuda_events():
+    import torch
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+# ---------------------------------------------------------------- TDVP workloads
+def build_specs(args, rank: int):
+    from qca_gb300 import workloads as W
+    if args.workload == "batched":
+        return W.chain_mix(args.chains, seed=1000 + rank), "batched 2TDVP: %d chains, N~U{16..96}, d in {1,2,3}, " \
+            "interval in {[1,1],[2,3],[2,4]}, chi in {32,64,128}, dt=0.05" % args.chains
+    spec = W.single_chain(64, 2, range(2, 4), 256, seed=64 + rank, dt=0.05, eps=1e-10)
+    return [spec], "single-chain 2TDVP: N=64, d=2, interval [2,3], chi=256, eps=1e-10, dt=0.05"
+
+
+def add_chains(eng, specs, precision_code, stream=None):
+    from qca_gb300 import _lib
+    from qca_gb300.algorithms import chain_desc
+    ids = []
+    for s in specs:
+        mps = s.mps()
+        d, keep = chain_desc(mps.A, s.mpo().W, s.algorithm, s.dt, s.chi, s.eps)
+        cid = ctypes.c_int(-1)
+        _lib.call("qca_chain_add", eng.h, ctypes.byref(d), _lib.stream_handle(stream), ctypes.byref(cid))
+        ids.append(cid.value)
+    return ids
+
+
+def get_mps(eng, cid, n):
+    from qca_gb300 import _lib
+    from qca_gb300.algorithms import unpack_mps
+    b = np.zeros(n + 1, dtype=np.int32)
+    _lib.call("qca_chain_bonds", eng.h, cid, b.ctypes.data_as(_lib._PI))
+    size = sum(2 * int(b[i]) * int(b[i + 1]) for i in range(n))
+    flat = np.zeros(size, dtype=np.complex128)
+    _lib.call("qca_chain_get_mps", eng.h, cid, flat.view(np.float64).ctypes.data_as(_lib._PD),
+              ctypes.c_size_t(2 * size), None)
+    return unpack_mps(flat, [int(x) for x in b])
+
+
+def cpu_tdvp_sample(specs, states, budget_s: float):
+    """Time the reference algorithm (oracle restatement of tdvp.py with dense H_eff
+    + eigh) on the host cores, on chains of the same workload starting from the
+    same states the GPU reached; returns (site-updates/s, description)."""
+    from oracle import qca_oracle as O
+    done_su, t_used, used = 0, 0.0, []
+    for spec, A in zip(specs, states):
+        W = O.build_mpo(O.Rules(spec.n, spec.interval, spec.distance))
+        t0 = time.perf_counter()
+        orc = O.TDVPOracle([a.copy() for a in A], W, spec.algorithm, spec.dt, spec.chi, spec.eps, fixed=True)
+        orc.step()
+        t_used += time.perf_counter() - t0
+        done_su += spec.site_updates_per_step()
+        used.append(f"N={spec.n},chi<={max(a.shape[2] for a in A)}")
+        if t_used > budget_s:
+            break
+    return done_su / t_used, "one oracle TDVP step (incl. init) of each of %d chains [%s] from the GPU's " \
+        "warmed-up states" % (len(used), "; ".join(used[:6]))
+
+
+def run_tdvp(args, dist: Dist):
+    import torch
+    from qca_gb300 import _lib
+    from qca_gb300.algorithms import _Engine
+    torch.cuda.set_device(dist.local)
+    prec = _lib.QCA_PREC_MIXED if args.precision == "mixed" else _lib.QCA_PREC_FP64
+    specs, desc = build_specs(args, dist.rank)
+    eng = _Engine(prec)
+    ids = add_chains(eng, specs, prec)
+    cids = (ctypes.c_int * len(ids))(*ids)
+    su_per_step = sum(s.site_updates_per_step() for s in specs)
+    # warm-up (bond dimensions grow from the product states)
+    _lib.call("qca_engine_step_chains", eng.h, cids, len(ids), args.warmup, None)
+    torch.cuda.synchronize()
+    _lib.call("qca_engine_profile", eng.h, 1)
+    kernel_stats(eng)  # reset
+    clocks = Clocks(dist.local)
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    e0, e1 = cuda_events()
+    e0.record()
+    _lib.call("qca_engine_step_chains", eng.h, cids, len(ids), args.steps, None)
+    e1.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    dist.barrier()
+    ms = dist.max(e0.elapsed_time(e1))
+    ks = kernel_stats(eng)
+    _lib.call("qca_engine_profile", eng.h, 0)
+    total_su = dist.sum(su_per_step * args.steps)
+    value = total_su / (ms / 1e3)
+    bonds = []
+    for cid, s in zip(ids, specs):
+        b = np.zeros(s.n + 1, dtype=np.int32)
+        _lib.call("qca_chain_bonds", eng.h, cid, b.ctypes.data_as(_lib._PI))
+        bonds.append(int(b.max()))
+    # dominant kernel class and its roofline
+    dom = max(ks, key=lambda k: ks[k]["ms"])
+    pk = peaks()
+    launches = int(sum(v["launches"] for v in ks.values()))
+    gemm = ks["gemm"]
+    tflops = gemm["flops"] / (gemm["ms"] / 1e3) / 1e12 if gemm["ms"] > 0 else 0.0
+    roofline = {"kernel": dom, "bound": "tensor",
+                "achieved": round(tflops, 3), "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                "frac": round(tflops / pk["bf16_tflops"], 5), "traffic": None,
+                "peak_source": f"{pk['source']} bf16 dense", "measured_kernel": "gemm",
+                "kernel_time_share": {k: round(v["ms"] / max(1e-9, sum(x["ms"] for x in ks.values())), 4)
+                                      for k, v in ks.items()}}
+    states = [get_mps(eng, cid, s.n) for cid, s in zip(ids[:8], specs[:8])]
+    # end to end through the public API with host buffers: upload the warmed-up
+    # states (pinned host -> device), evolve, read the populations every step
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(args, specs, [get_mps(eng, cid, s.n) for cid, s in zip(ids, specs)], prec, dist)
+    del eng
+    cpu = None
+    if not args.no_cpu and dist.rank == 0:
+        v, sample = cpu_tdvp_sample(specs, states, 15.0)
+        cpu = {"value": round(v, 3), "unit": "site-updates/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": sample}
+    line = {
+        "metric": "site-updates/s", "value": round(value, 2), "unit": "site-updates/s", "n_gpus": dist.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
+        "config": {"workload": desc, "precision": args.precision, "chains_per_gpu": len(specs),
+                   "site_updates_per_step": su_per_step, "max_bond_dim_reached": max(bonds),
+                   "l2": "working set larger than L2 (>= %.1f GB resident)" % (len(specs) * 0.01)},
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+    }
+    return line
+
+
+def run_e2e(args, specs, states, prec, dist: Dist):
+    import torch
+    from qca_gb300 import _lib
+    from qca_gb300.algorithms import _Engine, chain_desc
+    eng = _Engine(prec)
+    n_tot = sum(s.n for s in specs)
+    pop = np.zeros(n_tot)
+    dpop = np.zeros(n_tot)
+    sse = np.zeros(n_tot)
+    bd = np.zeros(n_tot + len(specs))
+    descs = [chain_desc(A, s.mpo().W, s.algorithm, s.dt, s.chi, s.eps) for s, A in zip(specs, states)]
+    h2d = sum(k[2].nbytes + k[3].nbytes for _, k in descs)
+    d2h = pop.nbytes + dpop.nbytes + sse.nbytes + bd.nbytes
+    dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ids = []
+    for d, _ in descs:
+        cid = ctypes.c_int(-1)
+        _lib.call("qca_chain_add", eng.h, ctypes.byref(d), None, ctypes.byref(cid))
+        ids.append(cid.value)
+    cids = (ctypes.c_int * len(ids))(*ids)
+    for _ in range(args.steps):
+        _lib.call("qca_engine_step_chains", eng.h, cids, len(ids), 1, None)
+        _lib.call("qca_engine_measure", eng.h, cids, len(ids), pop.ctypes.data_as(_lib._PD),
+                  dpop.ctypes.data_as(_lib._PD), sse.ctypes.data_as(_lib._PD), bd.ctypes.data_as(_lib._PD), None)
+    torch.cuda.synchronize()
+    el = dist.max(time.perf_counter() - t0)
+    su = dist.sum(sum(s.site_updates_per_step() for s in specs) * args.steps)
+    del eng
+    return {"value": round(su / el, 2), "unit": "site-updates/s", "h2d_bytes_per_step": int(h2d / args.steps),
+            "d2h_bytes_per_step": int(d2h), "includes": "chain upload + TDVP init, every step: step + measure "
+            "(populations, entropies, bond dims to host)"}
+
+
+# ---------------------------------------------------------------- exact workload
+def run_exact(args, dist: Dist):
+    import torch
+    import types
+    from qca_gb300 import GpuExact, MPO, MPS, Rules
+    from qca_gb300 import workloads as W
+    torch.cuda.set_device(dist.local)
+    n, d, lo, hi, dt, m = 24, 2, 2, 4, 0.05, 30
+    p = W.product_probabilities(np.random.default_rng(2024 + dist.rank), n)
+    H = MPO.hamiltonian_from_rules(Rules(n, range(lo, hi), d))
+    a = GpuExact(MPS.from_density_distribution(p), H, types.SimpleNamespace(
+        step_size=dt, algorithm="exact", precision=args.precision, krylov_dim=m))
+    a.evolve(args.warmup)
+    clocks = Clocks(dist.local)
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    e0, e1 = cuda_events()
+    e0.record()
+    a.evolve(args.steps)
+    e1.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = dist.max(e0.elapsed_time(e1))
+    amps = dist.sum((1 << n) * args.steps)
+    b = 16 if args.precision == "fp64" else 8
+    alg_bytes = (4 * m + 1) * (1 << n) * b
+    pk = peaks()
+    gbs = alg_bytes / (ms / args.steps / 1e3) / 1e9
+    # e2e: host state in, state out, through the public API
+    psi = a.state_vector()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        a.set_state_vector(psi)
+        a.do_time_step()
+        psi = a.state_vector()
+    el = time.perf_counter() - t0
+    line = {
+        "metric": "amplitude-updates/s", "value": round(amps / (ms / 1e3), 1), "unit": "amplitude-updates/s",
+        "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic",
+        "config": {"workload": "exact N=24, d=2, interval [2,3], Krylov 30, dt=0.05", "precision": args.precision,
+                   "l2": "state 2^24 amplitudes x 30 Krylov vectors > L2"},
+        "roofline": {"bound": "hbm", "achieved": round(gbs, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
+                     "frac": round(gbs / pk["hbm_gbs"], 4), "traffic": None,
+                     "note": "algorithmic bytes (4m+1) 2^N b per step over the whole step"},
+        "e2e": {"value": round((1 << n) * args.steps / el, 1), "unit": "amplitude-updates/s",
+                "h2d_bytes_per_step": 16 << n, "d2h_bytes_per_step": 16 << n},
+        "gpu_launches": args.steps * (2 + 30 * 4), "clocks": clk, "cpu_baseline": None,
+    }
+    return line
+
+
+# ---------------------------------------------------------------- reference arm
+def run_reference(args, dist: Dist):
+    if dist.rank != 0:
+        return None
+    from qca_gb300 import workloads as W
+    from oracle import qca_oracle as O
+    if args.workload == "exact":
+        n = 20  # the dense/sparse CPU path at 2^24 takes minutes per step; sample 2^20
+        p = W.product_probabilities(np.random.default_rng(2024), n)
+        psi = O.product_state_vector(p)
+        for _ in range(args.warmup):
+            psi = O.exact_evolve(psi, n, 2, range(2, 4), 0.05, 1)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            psi = O.exact_evolve(psi, n, 2, range(2, 4), 0.05, 1)
+        el = time.perf_counter() - t0
+        v = (1 << n) * args.steps / el
+        return {"impl": "reference", "metric": "amplitude-updates/s", "value": round(v, 1),
+                "unit": "amplitude-updates/s", "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
+                "higher_is_better": True, "config": {"workload": "exact, sampled at N=20 on the host"},
+                "cpu_baseline": {"value": round(v, 1), "unit": "amplitude-updates/s", "cores": os.cpu_count(),
+                                 "kind": "port", "sample": "sparse expm_multiply restatement at N=20"},
+                "e2e": {"value": round(v, 1), "unit": "amplitude-updates/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+    specs, desc = build_specs(args, 0)
+    # bounded sample per step: one reference TDVP step of one chain of the mix at
+    # the bond dimensions the workload reaches after the warm-up steps
+    spec = specs[0]
+    W_ = O.build_mpo(O.Rules(spec.n, spec.interval, spec.distance))
+    orc = O.TDVPOracle(O.mps_from_density_distribution(spec.p), W_, spec.algorithm, spec.dt, spec.chi, spec.eps)
+    for _ in range(args.warmup):
+        orc.step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        orc.step()
+    el = time.perf_counter() - t0
+    v = spec.site_updates_per_step() * args.steps / el
+    return {"impl": "reference", "metric": "site-updates/s", "value": round(v, 3), "unit": "site-updates/s",
+            "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(el / args.steps * 1e3, 2), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": {"workload": desc},
+            "cpu_baseline": {"value": round(v, 3), "unit": "site-updates/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": f"chain 0 of the mix (N={spec.n}, d={spec.distance}, chi cap {spec.chi}), "
+                                       f"oracle restatement of tdvp.py, {args.steps} steps after {args.warmup}"},
+            "e2e": {"value": round(v, 3), "unit": "site-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    dist = Dist(args.gpus)
+    if args.impl == "reference":
+        line = run_reference(args, dist)
+    elif args.workload == "exact":
+        line = run_exact(args, dist)
+    else:
+        line = run_tdvp(args, dist)
+    if dist.rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -125,6 +125,11 @@ int qca_engine_step_chains(qca_engine* e, const int* chain_ids, int count, int n
  * single_site_entropy[N], bond_dims[N+1] (any may be NULL). */
 int qca_chain_measure(qca_engine* e, int chain_id, double* population, double* d_population,
                       double* single_site_entropy, double* bond_dims, void* stream);
+/* Algorithm.measure for `count` chains at once (their QR sweeps run in lock step);
+ * the outputs are concatenated over the chains in the given order: N_c values per
+ * chain (N_c + 1 for bond_dims).  Mutates the gauges like qca_chain_measure. */
+int qca_engine_measure(qca_engine* e, const int* chain_ids, int count, double* population, double* d_population,
+                       double* single_site_entropy, double* bond_dims, void* stream);
 /* Current MPS bond dimensions D_0..D_N. */
 int qca_chain_bonds(qca_engine* e, int chain_id, int* bonds);
 /* psi getter (tdvp.py:42-44): the MPS tensors into host memory, concatenated like
@@ -133,6 +138,15 @@ int qca_chain_get_mps(qca_engine* e, int chain_id, double* mps, size_t capacity,
 /* Statistics of the last step of a chain: [0] largest Lanczos dimension used,
  * [1] summed discarded weight (sum of squared truncated singular values). */
 int qca_chain_stats(qca_engine* e, int chain_id, double* stats);
+
+/* Profiling hook (no counterpart in the reference, which has no tracing): when
+ * enabled, every grouped launch is bracketed by CUDA events on its stream.
+ * qca_engine_kernel_stats writes 7 kernel classes x 4 values
+ * (launches, milliseconds, algorithmic real flops, algorithmic bytes); classes:
+ * 0 GEMM contractions, 1 sparse MPO application, 2 Lanczos vector kernels,
+ * 3 Lanczos tridiagonal exponential, 4 SVD, 5 QR, 6 other. */
+int qca_engine_profile(qca_engine* e, int enable);
+int qca_engine_kernel_stats(qca_engine* e, double* out, int reset);
 
 #ifdef __cplusplus
 }

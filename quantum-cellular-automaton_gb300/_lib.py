@@ -92,9 +92,12 @@ SIGNATURES = {
     "qca_engine_step": [_P, _I, _P],
     "qca_engine_step_chains": [_P, _PI, _I, _I, _P],
     "qca_chain_measure": [_P, _I, _PD, _PD, _PD, _PD, _P],
+    "qca_engine_measure": [_P, _PI, _I, _PD, _PD, _PD, _PD, _P],
     "qca_chain_bonds": [_P, _I, _PI],
     "qca_chain_get_mps": [_P, _I, _PD, _SZ, _P],
     "qca_chain_stats": [_P, _I, _PD],
+    "qca_engine_profile": [_P, _I],
+    "qca_engine_kernel_stats": [_P, _PD, _I],
 }
 
 _lib = None

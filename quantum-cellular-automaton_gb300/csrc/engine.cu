@@ -167,6 +167,9 @@ struct Chain {
 // inside the owning chain's device allocation (or the engine's staging).  A failure
 // is returned as QCA_ERR_INVALID before anything is launched.
 // ---------------------------------------------------------------------------------
+// kernel classes reported by qca_engine_kernel_stats
+enum : int { KC_GEMM = 0, KC_WAPPLY, KC_LZVEC, KC_LZFIN, KC_SVD, KC_QR, KC_MISC, KC_N };
+
 struct Span {
   const char* lo;
   const char* hi;
@@ -190,10 +193,14 @@ struct EngineBase {
   virtual int remove(int id) = 0;
   virtual int step(const int* ids, int count, int nsteps, cudaStream_t st) = 0;
   virtual int measure(int id, double* pop, double* dpop, double* sse, double* bonds, cudaStream_t st) = 0;
+  virtual int measure_many(const int* ids, int count, double* pop, double* dpop, double* sse, double* bonds,
+                           cudaStream_t st) = 0;
   virtual int bonds(int id, int* out) = 0;
   virtual int get_mps(int id, double* out, size_t cap, cudaStream_t st) = 0;
   virtual int stats(int id, double* out) = 0;
   virtual std::vector<int> ids() const = 0;
+  virtual int kernel_stats(double* out, int reset) = 0;
+  virtual int set_profile(int on) = 0;
   size_t budget = 0, used = 0;
 };
 
@@ -215,7 +222,61 @@ struct Engine final : EngineBase {
   int done_cap = 0;
   cudaStream_t cur_st = nullptr;
 
+  // optional per-kernel-class timing with CUDA events (qca_engine_profile)
+  bool prof = false;
+  struct Pend {
+    int cls;
+    cudaEvent_t a, b;
+    double flops, bytes;
+  };
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  std::vector<Pend> pend;
+  double acc[KC_N][4] = {};
+
+  cudaEvent_t next_event() {
+    if (ev_used == ev_pool.size()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      ev_pool.push_back(e);
+    }
+    return ev_pool[ev_used++];
+  }
+  template <typename F>
+  int timed(int cls, double flops, double bytes, cudaStream_t st, F&& f) {
+    if (!prof) return f();
+    cudaEvent_t a = next_event(), b = next_event();
+    cudaEventRecord(a, st);
+    const int s = f();
+    cudaEventRecord(b, st);
+    pend.push_back(Pend{cls, a, b, flops, bytes});
+    return s;
+  }
+  void resolve() {
+    for (auto& p : pend) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, p.a, p.b);
+      acc[p.cls][0] += 1;
+      acc[p.cls][1] += ms;
+      acc[p.cls][2] += p.flops;
+      acc[p.cls][3] += p.bytes;
+    }
+    pend.clear();
+    ev_used = 0;
+  }
+  int kernel_stats(double* out, int reset) override {
+    for (int c = 0; c < KC_N; ++c)
+      for (int k = 0; k < 4; ++k) out[4 * c + k] = acc[c][k];
+    if (reset) memset(acc, 0, sizeof(acc));
+    return QCA_OK;
+  }
+  int set_profile(int on) override {
+    prof = on != 0;
+    return QCA_OK;
+  }
+
   ~Engine() override {
+    for (auto e : ev_pool) cudaEventDestroy(e);
     for (auto& kv : chains) cudaFree(kv.second->mem);
     cudaFreeHost(h_stage);
     cudaFree(d_stage);
@@ -241,6 +302,7 @@ struct Engine final : EngineBase {
   int sync(cudaStream_t st) {
     QCA_CUDA(cudaStreamSynchronize(st));
     stage_off = 0;
+    if (!pend.empty()) resolve();
     return QCA_OK;
   }
 
@@ -299,7 +361,13 @@ struct Engine final : EngineBase {
     }
     const GemmDesc<T>* dd;
     QCA_TRY(upload(v, st, &dd));
-    return launch_gemm<T>(dd, v.data(), (int)v.size(), cfg, st);
+    double fl = 0.0, by = 0.0;
+    for (auto& d : v) {
+      const double nb = (double)d.nb1 * d.nb2 * d.G;
+      fl += 8.0 * d.M * d.N * (double)d.K * nb;
+      by += sizeof(cplx<T>) * ((double)d.M * d.K * nb + (double)d.K * d.N * nb + (double)d.M * d.N * d.nb1 * d.nb2);
+    }
+    return timed(KC_GEMM, fl, by, st, [&] { return launch_gemm<T>(dd, v.data(), (int)v.size(), cfg, st); });
   }
 
   int run_wapply(std::vector<WapplyDesc<T>>& v, cudaStream_t st) {
@@ -316,7 +384,9 @@ struct Engine final : EngineBase {
     }
     const WapplyDesc<T>* dd;
     QCA_TRY(upload(v, st, &dd));
-    return launch_wapply<T>(dd, v.data(), (int)v.size(), st);
+    double by = 0.0;
+    for (auto& d : v) by += 2.0 * sizeof(cplx<T>) * d.nout * (double)d.blk;
+    return timed(KC_WAPPLY, 0.0, by, st, [&] { return launch_wapply<T>(dd, v.data(), (int)v.size(), st); });
   }
 
   int run_copy(std::vector<CopyDesc<T>>& v, cudaStream_t st) {
@@ -334,7 +404,7 @@ struct Engine final : EngineBase {
     }
     const CopyDesc<T>* dd;
     QCA_TRY(upload(v, st, &dd));
-    return launch_copy<T>(dd, v.data(), (int)v.size(), st);
+    return timed(KC_MISC, 0.0, 0.0, st, [&] { return launch_copy<T>(dd, v.data(), (int)v.size(), st); });
   }
 
   static GemmDesc<T> gemm0() {
@@ -495,17 +565,20 @@ struct Engine final : EngineBase {
     }
     const LanczosDesc<T>* dd;
     QCA_TRY(upload(L, st, &dd));
-    QCA_TRY(launch_lz_init<T>(dd, L.data(), nd, mmax, lz_tol, st));
+    QCA_TRY(timed(KC_LZVEC, 0, 0, st, [&] { return launch_lz_init<T>(dd, L.data(), nd, mmax, lz_tol, st); }));
     int j = 0;
     for (; j < mmax; ++j) {
       QCA_TRY(matvec(P, j, st));
       // the descriptor copy may have been recycled by a staging reset
       QCA_TRY(upload(L, st, &dd));
-      QCA_TRY(launch_lz_orth_pass<T>(dd, L.data(), nd, j, 0, st));
-      QCA_TRY(launch_lz_orth_pass<T>(dd, L.data(), nd, j, 1, st));
-      QCA_TRY(launch_lz_orth_pass<T>(dd, L.data(), nd, j, 2, st));
-      QCA_TRY(launch_lz_finalize_j<T>(dd, nd, j, mmax, st));
-      QCA_TRY(launch_lz_normalize<T>(dd, L.data(), nd, j, st));
+      QCA_TRY(timed(KC_LZVEC, 0, 0, st, [&] {
+        int s = launch_lz_orth_pass<T>(dd, L.data(), nd, j, 0, st);
+        if (s == QCA_OK) s = launch_lz_orth_pass<T>(dd, L.data(), nd, j, 1, st);
+        if (s == QCA_OK) s = launch_lz_orth_pass<T>(dd, L.data(), nd, j, 2, st);
+        return s;
+      }));
+      QCA_TRY(timed(KC_LZFIN, 0, 0, st, [&] { return launch_lz_finalize_j<T>(dd, nd, j, mmax, st); }));
+      QCA_TRY(timed(KC_LZVEC, 0, 0, st, [&] { return launch_lz_normalize<T>(dd, L.data(), nd, j, st); }));
       const bool check = (j >= 3 && (j % 3 == 0)) || j + 1 == mmax;
       if (check) {
         QCA_CUDA(cudaMemcpyAsync(h_done, d_done, sizeof(int) * nd, cudaMemcpyDeviceToHost, st));
@@ -516,7 +589,7 @@ struct Engine final : EngineBase {
       }
     }
     QCA_TRY(upload(L, st, &dd));
-    QCA_TRY(launch_lz_combine<T>(dd, L.data(), nd, st));
+    QCA_TRY(timed(KC_LZVEC, 0, 0, st, [&] { return launch_lz_combine<T>(dd, L.data(), nd, st); }));
     for (auto& p : P) p.c->lz_used = std::max(p.c->lz_used, std::min(j + 2, mmax));
     return QCA_OK;
   }
@@ -743,7 +816,7 @@ struct Engine final : EngineBase {
     QCA_TRY(check_qr(q));
     const QrDesc<T>* dq;
     QCA_TRY(upload(q, st, &dq));
-    QCA_TRY(launch_qr<T>(dq, (int)q.size(), st));
+    QCA_TRY(timed(KC_QR, 0, 0, st, [&] { return launch_qr<T>(dq, (int)q.size(), st); }));
     QCA_TRY(run_gemm(g, st));
     for (auto& jb : J) {
       Chain<T>* c = jb.c;
@@ -945,13 +1018,13 @@ struct Engine final : EngineBase {
       QCA_TRY(check_svd(sv));
       const SvdDesc<T>* ds;
       QCA_TRY(upload(sv, st, &ds));
-      QCA_TRY(launch_svd<T>(ds, (int)sv.size(), st));
+      QCA_TRY(timed(KC_SVD, 0, 0, st, [&] { return launch_svd<T>(ds, (int)sv.size(), st); }));
     }
     if (!qr.empty()) {
       QCA_TRY(check_qr(qr));
       const QrDesc<T>* dq;
       QCA_TRY(upload(qr, st, &dq));
-      QCA_TRY(launch_qr<T>(dq, (int)qr.size(), st));
+      QCA_TRY(timed(KC_QR, 0, 0, st, [&] { return launch_qr<T>(dq, (int)qr.size(), st); }));
     }
     if (!svc.empty()) {
       for (size_t i = 0; i < svc.size(); ++i)
@@ -1174,52 +1247,79 @@ struct Engine final : EngineBase {
     return QCA_OK;
   }
 
-  int measure(int id, double* pop, double* dpop, double* sse, double* bonds_out, cudaStream_t st) override {
-    auto it = chains.find(id);
-    if (it == chains.end()) {
-      set_error("unknown chain %d", id);
-      return QCA_ERR_INVALID;
-    }
-    Chain<T>* c = it->second.get();
-    const int N = c->N;
-    // bond dims before the canonical sweep (mps.py:106-109)
-    if (bonds_out)
-      for (int i = 0; i <= N; ++i) bonds_out[i] = c->D[i];
-    std::vector<Chain<T>*> one{c};
-    if (c->center != 0) {
-      for (int k = c->center; k >= 1; --k) {
-        std::vector<MoveJob> J{MoveJob{c, k, false}};
-        QCA_TRY(qr_moves(J, st));
+  // Algorithm.measure for several chains in lock step (mps.py:100-140): bond dims,
+  // make_site_canonical(0), then a left QR sweep with the 2x2 density matrix of
+  // every site; mutates the gauge like the reference.  Outputs are concatenated
+  // over the chains in the given order (N_c values per chain, N_c + 1 for bonds).
+  int measure_many(const int* ids, int count, double* pop, double* dpop, double* sse, double* bonds_out,
+                   cudaStream_t st) override {
+    std::vector<Chain<T>*> C;
+    for (int i = 0; i < count; ++i) {
+      auto it = chains.find(ids[i]);
+      if (it == chains.end()) {
+        set_error("unknown chain %d", ids[i]);
+        return QCA_ERR_INVALID;
       }
+      C.push_back(it->second.get());
     }
-    std::vector<double> rho(4 * N);
-    double* drho = c->dscal + 8;
-    for (int s = 0; s < N; ++s) {
+    size_t ob = 0;
+    for (auto* c : C) {
+      if (bonds_out)
+        for (int i = 0; i <= c->N; ++i) bonds_out[ob + i] = c->D[i];
+      ob += c->N + 1;
+    }
+    int maxN = 0;
+    for (auto* c : C) maxN = std::max(maxN, c->N);
+    for (int k = maxN - 1; k >= 1; --k) {
+      std::vector<MoveJob> J;
+      for (auto* c : C)
+        if (k < c->N && k <= c->center) J.push_back(MoveJob{c, k, false});
+      QCA_TRY(qr_moves(J, st));
+    }
+    for (int s = 0; s < maxN; ++s) {
       if (s > 0) {
-        std::vector<MoveJob> J{MoveJob{c, s - 1, true}};
+        std::vector<MoveJob> J;
+        for (auto* c : C)
+          if (s < c->N) J.push_back(MoveJob{c, s - 1, true});
         QCA_TRY(qr_moves(J, st));
       }
-      QCA_TRY(launch_rho<T>(c->cur(s), c->D[s], c->D[s + 1], drho + 4 * s, st));
+      for (auto* c : C)
+        if (s < c->N)
+          QCA_TRY(timed(KC_MISC, 0, 0, st, [&] { return launch_rho<T>(c->cur(s), c->D[s], c->D[s + 1], c->dscal + 8 + 4 * s, st); }));
     }
-    QCA_CUDA(cudaMemcpyAsync(rho.data(), drho, sizeof(double) * 4 * N, cudaMemcpyDeviceToHost, st));
+    std::vector<std::vector<double>> rho(C.size());
+    for (size_t i = 0; i < C.size(); ++i) {
+      rho[i].resize(4 * C[i]->N);
+      QCA_CUDA(cudaMemcpyAsync(rho[i].data(), C[i]->dscal + 8, sizeof(double) * 4 * C[i]->N, cudaMemcpyDeviceToHost, st));
+    }
     QCA_TRY(sync(st));
-    c->center = N - 1;
-    for (int s = 0; s < N; ++s) {
-      const double r00 = rho[4 * s], r11 = rho[4 * s + 1], rr = rho[4 * s + 2], ri = rho[4 * s + 3];
-      if (pop) pop[s] = r11;
-      if (dpop) dpop[s] = std::nearbyint(r11);
-      if (sse) {
-        // eigenvalues of [[r00, r01], [conj r01, r11]]
-        const double tr = r00 + r11, det = r00 * r11 - (rr * rr + ri * ri);
-        const double disc = std::sqrt(std::max(0.0, tr * tr / 4 - det));
-        const double l1 = tr / 2 + disc, l2 = tr / 2 - disc;
-        double h = 0.0;
-        if (l1 > 0) h -= l1 * std::log2(l1);
-        if (l2 > 0) h -= l2 * std::log2(l2);
-        sse[s] = h;
+    size_t o = 0;
+    for (size_t i = 0; i < C.size(); ++i) {
+      Chain<T>* c = C[i];
+      c->center = c->N - 1;
+      for (int s = 0; s < c->N; ++s) {
+        const double* r = rho[i].data() + 4 * s;
+        const double r00 = r[0], r11 = r[1], rr = r[2], ri = r[3];
+        if (pop) pop[o + s] = r11;
+        if (dpop) dpop[o + s] = std::nearbyint(r11);
+        if (sse) {
+          // eigenvalues of [[r00, r01], [conj r01, r11]]; -sum l log2 l with 0 log 0 = 0
+          const double tr = r00 + r11, det = r00 * r11 - (rr * rr + ri * ri);
+          const double disc = std::sqrt(std::max(0.0, tr * tr / 4 - det));
+          const double l1 = tr / 2 + disc, l2 = tr / 2 - disc;
+          double h = 0.0;
+          if (l1 > 0) h -= l1 * std::log2(l1);
+          if (l2 > 0) h -= l2 * std::log2(l2);
+          sse[o + s] = h;
+        }
       }
+      o += c->N;
     }
     return QCA_OK;
+  }
+
+  int measure(int id, double* pop, double* dpop, double* sse, double* bonds_out, cudaStream_t st) override {
+    return measure_many(&id, 1, pop, dpop, sse, bonds_out, st);
   }
 
   int bonds(int id, int* out) override {
@@ -1623,6 +1723,16 @@ int qca_chain_measure(qca_engine* e, int chain_id, double* population, double* d
   return e->impl->measure(chain_id, population, d_population, single_site_entropy, bond_dims, (cudaStream_t)stream);
 }
 
+int qca_engine_measure(qca_engine* e, const int* chain_ids, int count, double* population, double* d_population,
+                       double* single_site_entropy, double* bond_dims, void* stream) {
+  if (!e || !chain_ids || count < 0) {
+    set_error("qca_engine_measure: invalid arguments");
+    return QCA_ERR_INVALID;
+  }
+  return e->impl->measure_many(chain_ids, count, population, d_population, single_site_entropy, bond_dims,
+                               (cudaStream_t)stream);
+}
+
 int qca_chain_bonds(qca_engine* e, int chain_id, int* bonds) {
   if (!e || !bonds) {
     set_error("qca_chain_bonds: NULL argument");
@@ -1637,6 +1747,22 @@ int qca_chain_get_mps(qca_engine* e, int chain_id, double* mps, size_t capacity,
     return QCA_ERR_INVALID;
   }
   return e->impl->get_mps(chain_id, mps, capacity, (cudaStream_t)stream);
+}
+
+int qca_engine_profile(qca_engine* e, int enable) {
+  if (!e) {
+    set_error("qca_engine_profile: NULL engine");
+    return QCA_ERR_INVALID;
+  }
+  return e->impl->set_profile(enable);
+}
+
+int qca_engine_kernel_stats(qca_engine* e, double* out, int reset) {
+  if (!e || !out) {
+    set_error("qca_engine_kernel_stats: NULL argument");
+    return QCA_ERR_INVALID;
+  }
+  return e->impl->kernel_stats(out, reset);
 }
 
 int qca_chain_stats(qca_engine* e, int chain_id, double* stats) {
