@@ -1018,7 +1018,12 @@ struct Engine final : EngineBase {
       QCA_TRY(check_svd(sv));
       const SvdDesc<T>* ds;
       QCA_TRY(upload(sv, st, &ds));
-      QCA_TRY(timed(KC_SVD, 0, 0, st, [&] { return launch_svd<T>(ds, (int)sv.size(), st); }));
+      double fl = 0.0;
+      for (auto& d : sv) {  // Golub-Van Loan thin-SVD count, x4 for complex
+        const double m = 2.0 * std::max(d.Dl, d.Dr), n = 2.0 * std::min(d.Dl, d.Dr);
+        fl += 4.0 * (4.0 * m * m * n + 8.0 * m * n * n + 9.0 * n * n * n);
+      }
+      QCA_TRY(timed(KC_SVD, fl, 0, st, [&] { return launch_svd<T>(ds, sv.data(), (int)sv.size(), st); }));
     }
     if (!qr.empty()) {
       QCA_TRY(check_qr(qr));
@@ -1040,6 +1045,10 @@ struct Engine final : EngineBase {
         }
         if (h_k[2 * i + 1]) c->status = h_k[2 * i + 1];
         c->D[l + 1] = k;
+      }
+      for (size_t i = 0; i < svc.size(); ++i) {
+        Chain<T>* c = svc[i];
+        const int l = c->dir == 0 ? c->pos : c->pos - 1;
         c->par[l] ^= 1;
         c->par[l + 1] ^= 1;
       }

@@ -1,15 +1,27 @@
 // Two-site split of 2TDVP (tdvp.py:286-296): SVD of theta viewed as the
 // (2 Dl) x (2 Dr) matrix Theta[(s1,a),(s2,c)], truncation to
 //   k = min{ i : ||s[i:]||_2 < eps }  capped at min(chi, len s)
-// and the new site tensors (right sweep: A_l = U, A_r = diag(s) Vh;
-// left sweep: A_l = U diag(s), A_r = Vh) with s renormalised (lautils.normalize).
+// and s renormalised (lautils.normalize, lautils.py:4-5).
 //
-// One CTA per problem runs a one-sided (Hestenes) Jacobi SVD on the narrower
-// orientation X (mx >= nx columns): column pairs are rotated in parallel in a
-// round-robin tournament until every pair is orthogonal to working precision.
-// Singular values are the FP64 norms of the final columns; the tail sums of the
-// truncation rule are accumulated in FP64.
+// One-sided (Hestenes) Jacobi on the narrower orientation W (mx >= nx):
+// W = Theta when 2 Dr <= 2 Dl, else W = Theta^H.  Its columns are distributed
+// over the shared memory of a thread-block cluster (1..16 CTAs, distributed
+// shared memory); in every round of a round-robin tournament each warp rotates
+// one disjoint column pair, reading and writing both columns through DSMEM, and
+// the cluster barrier separates the rounds.  The same rotations accumulate V
+// (nx x nx), kept beside X in distributed shared memory when the cluster has
+// room and in global memory otherwise.  At convergence X = W V has orthogonal
+// columns whose FP64 norms are the singular values; the site tensors are written
+// directly from X and V:
+//   W = Theta:    U = X / sigma,  Vh = V^H
+//   W = Theta^H:  U = V,          Vh = (X / sigma)^H
+// with the renormalised singular values multiplied into A_r (right sweep) or
+// A_l (left sweep), tdvp.py:121-122 and 141-142.
+#include <cooperative_groups.h>
+
 #include "tdvp_kernels.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace qca {
 
@@ -17,24 +29,30 @@ namespace {
 
 constexpr int kSvdThreads = 1024;
 constexpr int kSvdMaxN = 1024;
+constexpr int kSvdMaxSweeps = 30;
 
 template <typename T>
-struct Eps;
+struct Prec;
 template <>
-struct Eps<double> {
-  static constexpr double v = 1e-15;
+struct Prec<double> {
+  static constexpr double eps = 2.2e-16;
 };
 template <>
-struct Eps<float> {
-  static constexpr double v = 1e-7;
+struct Prec<float> {
+  static constexpr double eps = 1.2e-7;
 };
 
 template <typename T>
-__global__ void __launch_bounds__(kSvdThreads) svd_kernel(const SvdDesc<T>* __restrict__ descs) {
-  const SvdDesc<T>& D = descs[blockIdx.x];
-  __shared__ double snorm[kSvdMaxN];
-  __shared__ int perm[kSvdMaxN];
-  __shared__ int s_rot;
+__global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<T>* __restrict__ descs, int cs,
+                                                                  int cpc, int v_smem) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const SvdDesc<T>& D = descs[blockIdx.x / cs];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx<T>* Xloc = reinterpret_cast<cplx<T>*>(smem_raw);  // cpc columns of mx elements
+  __shared__ double snorm[kSvdMaxN];                     // used in CTA 0
+  __shared__ int perm[kSvdMaxN];                         // used in CTA 0
+  __shared__ int s_flag[2];                              // rotation flags (CTA 0), by sweep parity
   __shared__ int s_k;
   __shared__ double s_keep;
   const int Dl = D.Dl, Dr = D.Dr;
@@ -42,35 +60,40 @@ __global__ void __launch_bounds__(kSvdThreads) svd_kernel(const SvdDesc<T>* __re
   const bool trans = n > m;
   const int mx = trans ? n : m;
   const int nx = trans ? m : n;
-  cplx<T>* X = D.work;                   // column-major mx x nx
-  cplx<T>* V = D.work + (long long)mx * nx;  // column-major nx x nx
   const long long blk = (long long)Dl * Dr;
-  // load X and V = I
-  for (long long e = threadIdx.x; e < (long long)mx * nx; e += blockDim.x) {
-    const int col = (int)(e / mx), row = (int)(e - (long long)col * mx);
-    // Theta(r, c): r = (s1, a), c = (s2, cc)
-    const int r = trans ? col : row;
-    const int c = trans ? row : col;
-    const int s1 = r / Dl, a = r - s1 * Dl, s2 = c / Dr, cc = c - s2 * Dr;
-    cplx<T> v = D.theta[(long long)(s1 * 2 + s2) * blk + (long long)a * Dr + cc];
-    if (trans) v.im = -v.im;
-    X[e] = v;
+  // V columns: after X in shared memory, or slot-major in the global workspace
+  cplx<T>* Vloc = v_smem ? Xloc + (long long)cpc * mx : D.work + (long long)rank * cpc * nx;
+  for (int lc = 0; lc < cpc; ++lc) {
+    const int col = rank * cpc + lc;
+    if (col >= nx) break;
+    for (int row = threadIdx.x; row < nx; row += blockDim.x)
+      Vloc[(long long)lc * nx + row] = mk<T>(row == col ? (T)1 : (T)0, (T)0);
   }
-  for (long long e = threadIdx.x; e < (long long)nx * nx; e += blockDim.x) {
-    const int col = (int)(e / nx), row = (int)(e - (long long)col * nx);
-    V[e] = mk<T>(row == col ? (T)1 : (T)0, (T)0);
+  // load my columns of W
+  for (int lc = 0; lc < cpc; ++lc) {
+    const int col = rank * cpc + lc;
+    if (col >= nx) break;
+    for (int row = threadIdx.x; row < mx; row += blockDim.x) {
+      const int r = trans ? col : row;
+      const int c = trans ? row : col;
+      const int s1 = r / Dl, a = r - s1 * Dl, s2 = c / Dr, cc = c - s2 * Dr;
+      cplx<T> v = D.theta[(long long)(s1 * 2 + s2) * blk + (long long)a * Dr + cc];
+      if (trans) v.im = -v.im;
+      Xloc[(long long)lc * mx + row] = v;
+    }
   }
-  __syncthreads();
+  if (threadIdx.x < 2) s_flag[threadIdx.x] = 0;
+  cluster.sync();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int P = nx + (nx & 1);
-  const double tol = Eps<T>::v * 4.0;
+  const double tol = Prec<T>::eps * fmax(8.0, 2.0 * sqrt((double)mx));
+  int* flag0 = cluster.map_shared_rank(s_flag, 0);
   int sweep = 0;
-  for (; sweep < 40; ++sweep) {
-    if (threadIdx.x == 0) s_rot = 0;
-    __syncthreads();
+  for (; sweep < kSvdMaxSweeps; ++sweep) {
+    const int par = sweep & 1;
     int rotated = 0;
     for (int round = 0; round < P - 1; ++round) {
-      for (int pk = wid; pk < P / 2; pk += nw) {
+      for (int pk = rank + cs * wid; pk < P / 2; pk += cs * nw) {
         int p, q;
         if (pk == 0) {
           p = P - 1;
@@ -85,158 +108,228 @@ __global__ void __launch_bounds__(kSvdThreads) svd_kernel(const SvdDesc<T>* __re
           p = q;
           q = t;
         }
-        cplx<T>* xp = X + (long long)p * mx;
-        cplx<T>* xq = X + (long long)q * mx;
-        double al = 0.0, be = 0.0, gr = 0.0, gi = 0.0;
+        cplx<T>* xp = cluster.map_shared_rank(Xloc, p / cpc) + (long long)(p % cpc) * mx;
+        cplx<T>* xq = cluster.map_shared_rank(Xloc, q / cpc) + (long long)(q % cpc) * mx;
+        // pair Gram entries and the rotation in the working precision T (the
+        // singular values are re-evaluated in FP64 after convergence)
+        T al = 0, be = 0, gr = 0, gi = 0;
         for (int i = lane; i < mx; i += 32) {
           const cplx<T> u = xp[i], v = xq[i];
-          al += (double)u.re * u.re + (double)u.im * u.im;
-          be += (double)v.re * v.re + (double)v.im * v.im;
-          gr += (double)u.re * v.re + (double)u.im * v.im;  // conj(u) v
-          gi += (double)u.re * v.im - (double)u.im * v.re;
+          al = fma(u.re, u.re, fma(u.im, u.im, al));
+          be = fma(v.re, v.re, fma(v.im, v.im, be));
+          gr = fma(u.re, v.re, fma(u.im, v.im, gr));   // conj(u) v
+          gi = fma(u.re, v.im, fma(-u.im, v.re, gi));
         }
-        al = warp_sum(al);
-        be = warp_sum(be);
-        gr = warp_sum(gr);
-        gi = warp_sum(gi);
-        const double g = sqrt(gr * gr + gi * gi);
-        if (!(g > tol * sqrt(al * be)) || g == 0.0) continue;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          al += __shfl_xor_sync(0xffffffffu, al, o);
+          be += __shfl_xor_sync(0xffffffffu, be, o);
+          gr += __shfl_xor_sync(0xffffffffu, gr, o);
+          gi += __shfl_xor_sync(0xffffffffu, gi, o);
+        }
+        const T g = sqrt(gr * gr + gi * gi);
+        if (!(g > (T)tol * sqrt(al * be))) continue;
         rotated = 1;
-        const double zeta = (be - al) / (2.0 * g);
-        const double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-        const double c = 1.0 / sqrt(1.0 + t * t);
-        const double s = c * t;
-        const double er = gr / g, ei = gi / g;  // e^{i phi}
-        // x_p' = c x_p - s e^{-i phi} x_q ; x_q' = s e^{i phi} x_p + c x_q
-        const T cc = (T)c;
-        const cplx<T> smq = mk<T>((T)(-s * er), (T)(s * ei));   // -s e^{-i phi}
-        const cplx<T> spq = mk<T>((T)(s * er), (T)(s * ei));    // s e^{i phi}
+        const T zeta = (be - al) / (2 * g);
+        const T t = (zeta >= 0 ? (T)1 : (T)-1) / (fabs(zeta) + sqrt(1 + zeta * zeta));
+        const T c = 1 / sqrt(1 + t * t);
+        const T s = c * t;
+        const T er = gr / g, ei = gi / g;  // e^{i phi}
+        // x_p' = c x_p - s e^{-i phi} x_q ; x_q' = s e^{i phi} x_p + c x_q  (unitary)
+        const T cc = c;
+        const cplx<T> smq = mk<T>(-s * er, s * ei);
+        const cplx<T> spq = mk<T>(s * er, s * ei);
         for (int i = lane; i < mx; i += 32) {
           const cplx<T> u = xp[i], v = xq[i];
           xp[i] = cc * u + smq * v;
           xq[i] = spq * u + cc * v;
         }
-        cplx<T>* vp = V + (long long)p * nx;
-        cplx<T>* vq = V + (long long)q * nx;
+        cplx<T>* vp = (v_smem ? cluster.map_shared_rank(Xloc, p / cpc) + (long long)cpc * mx
+                              : D.work + (long long)(p / cpc) * cpc * nx) + (long long)(p % cpc) * nx;
+        cplx<T>* vq = (v_smem ? cluster.map_shared_rank(Xloc, q / cpc) + (long long)cpc * mx
+                              : D.work + (long long)(q / cpc) * cpc * nx) + (long long)(q % cpc) * nx;
         for (int i = lane; i < nx; i += 32) {
           const cplx<T> u = vp[i], v = vq[i];
           vp[i] = cc * u + smq * v;
           vq[i] = spq * u + cc * v;
         }
       }
-      __syncthreads();
+      cluster.sync();
     }
-    if (rotated) s_rot = 1;
-    __syncthreads();
-    if (!s_rot) break;
-    __syncthreads();
+    if (rotated && lane == 0) atomicOr(flag0 + par, 1);
+    cluster.sync();
+    const int any = *(volatile int*)(flag0 + par);
+    cluster.sync();  // everyone has read the flag before it is reset below
+    if (rank == 0 && threadIdx.x == 0) s_flag[par] = 0;
+    if (!any) break;
   }
-  // singular values (FP64 column norms) and descending order
-  for (int j = wid; j < nx; j += nw) {
-    const cplx<T>* xj = X + (long long)j * mx;
+  // column norms (FP64) gathered in CTA 0
+  double* snorm0 = cluster.map_shared_rank(snorm, 0);
+  for (int lc = wid; lc < cpc; lc += nw) {
+    const int col = rank * cpc + lc;
+    if (col >= nx) break;
+    const cplx<T>* x = Xloc + (long long)lc * mx;
     double s = 0.0;
-    for (int i = lane; i < mx; i += 32) s += (double)xj[i].re * xj[i].re + (double)xj[i].im * xj[i].im;
+    for (int i = lane; i < mx; i += 32) s += (double)x[i].re * x[i].re + (double)x[i].im * x[i].im;
     s = warp_sum(s);
-    if (lane == 0) snorm[j] = sqrt(s);
+    if (lane == 0) snorm0[col] = sqrt(s);
   }
-  __syncthreads();
-  for (int j = threadIdx.x; j < nx; j += blockDim.x) {
-    const double sj = snorm[j];
-    int rank = 0;
-    for (int i = 0; i < nx; ++i) {
-      const double si = snorm[i];
-      rank += (si > sj) || (si == sj && i < j);
+  cluster.sync();
+  if (rank == 0) {
+    for (int j = threadIdx.x; j < nx; j += blockDim.x) {
+      const double sj = snorm[j];
+      int r = 0;
+      for (int i = 0; i < nx; ++i) {
+        const double si = snorm[i];
+        r += (si > sj) || (si == sj && i < j);
+      }
+      perm[r] = j;
     }
-    perm[rank] = j;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    // tail norms ||s[i:]|| in FP64; first i below eps (tdvp.py:290-292)
-    const int len = nx;
-    int k = len;
-    double tail = 0.0, total = 0.0;
-    for (int i = len - 1; i >= 0; --i) total += snorm[perm[i]] * snorm[perm[i]];
-    double acc = 0.0;
-    int first = len;
-    for (int i = len - 1; i >= 0; --i) {
-      acc += snorm[perm[i]] * snorm[perm[i]];
-      if (sqrt(acc) < D.eps) first = i;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      // tail norms ||s[i:]|| in FP64 (tdvp.py:290-292)
+      double acc = 0.0, total = 0.0;
+      int first = nx;
+      for (int i = nx - 1; i >= 0; --i) {
+        const double sv = snorm[perm[i]];
+        acc += sv * sv;
+        if (sqrt(acc) < D.eps) first = i;
+      }
+      total = acc;
+      int k = first;
+      const int cap = D.chi < nx ? D.chi : nx;
+      if (k > cap) k = cap;
+      if (k > D.kmax) k = D.kmax;
+      if (k < 1) k = 1;
+      double keep = 0.0;
+      for (int i = 0; i < k; ++i) keep += snorm[perm[i]] * snorm[perm[i]];
+      s_k = k;
+      s_keep = sqrt(keep);
+      *D.k_out = k;
+      if (D.discarded) *D.discarded += total > 0 ? (total - keep) / total : 0.0;
+      for (int i = 0; i < nx; ++i) D.sv[i] = snorm[perm[i]];
+      if (D.status) *D.status = (sweep >= kSvdMaxSweeps) ? QCA_ERR_NOT_CONVERGED : 0;
     }
-    k = first;
-    const int cap = D.chi < len ? D.chi : len;
-    if (k > cap) k = cap;
-    if (k > D.kmax) k = D.kmax;
-    if (k < 1) k = 1;
-    double keep = 0.0;
-    for (int i = 0; i < k; ++i) keep += snorm[perm[i]] * snorm[perm[i]];
-    tail = total - keep;
-    s_k = k;
-    s_keep = sqrt(keep);
-    *D.k_out = k;
-    if (D.discarded) *D.discarded += total > 0 ? tail / total : 0.0;
-    for (int i = 0; i < len; ++i) D.sv[i] = snorm[perm[i]];
-    if (D.status) *D.status = (sweep >= 40) ? QCA_ERR_NOT_CONVERGED : 0;
   }
-  __syncthreads();
-  const int k = s_k;
-  const double keep = s_keep;
-  // U (m x k) and Vh (k x n) of Theta
-  //  not trans: U[:, i] = X[:, perm i] / sigma, Vh[i, c] = conj(V[c, perm i])
-  //  trans:     U[:, i] = V[:, perm i],          Vh[i, c] = conj(X[c, perm i]) / sigma
-  for (long long e = threadIdx.x; e < (long long)m * k; e += blockDim.x) {
-    const int i = (int)(e % k);
-    const int r = (int)(e / k);
-    const int j = perm[i];
-    const double sig = snorm[j];
-    cplx<T> u;
+  cluster.sync();
+  const int k = *cluster.map_shared_rank(&s_k, 0);
+  const double keep = *cluster.map_shared_rank(&s_keep, 0);
+  const int* perm0 = cluster.map_shared_rank(perm, 0);
+  const double* sn0 = cluster.map_shared_rank(snorm, 0);
+  // kept columns that live in this CTA
+  for (int i = 0; i < k; ++i) {
+    const int j = perm0[i];
+    if (j / cpc != rank) continue;
+    const cplx<T>* x = Xloc + (long long)(j % cpc) * mx;
+    const cplx<T>* v = Vloc + (long long)(j % cpc) * nx;
+    const double sig = sn0[j];
+    const double inv = sig > 0 ? 1.0 / sig : 0.0;
+    const double sn = keep > 0 ? sig / keep : 0.0;  // renormalised singular value
+    const double fl = D.right_sweep ? 1.0 : sn;     // scale of A_l
+    const double fr = D.right_sweep ? sn : 1.0;     // scale of A_r
     if (!trans) {
-      const cplx<T> x = X[(long long)j * mx + r];
-      const double f = sig > 0 ? 1.0 / sig : 0.0;
-      u = mk<T>((T)(x.re * f), (T)(x.im * f));
+      // U[:, i] = x / sigma over the m = mx rows (row = s1 * Dl + a); Vh[i, c] = conj(v[c])
+      for (int row = threadIdx.x; row < mx; row += blockDim.x) {
+        const cplx<T> u = x[row];
+        const double f = inv * fl;
+        D.Al[(long long)row * k + i] = mk<T>((T)(u.re * f), (T)(u.im * f));
+      }
+      for (int c = threadIdx.x; c < nx; c += blockDim.x) {
+        const cplx<T> u = v[c];
+        const int s2 = c / Dr, cc = c - s2 * Dr;
+        D.Ar[((long long)s2 * k + i) * Dr + cc] = mk<T>((T)(u.re * fr), (T)(-u.im * fr));
+      }
     } else {
-      u = V[(long long)j * nx + r];
+      // U[:, i] = v over the m = nx rows; Vh[i, c] = conj(x[c]) / sigma over the n = mx columns
+      for (int row = threadIdx.x; row < nx; row += blockDim.x) {
+        const cplx<T> u = v[row];
+        D.Al[(long long)row * k + i] = mk<T>((T)(u.re * fl), (T)(u.im * fl));
+      }
+      for (int c = threadIdx.x; c < mx; c += blockDim.x) {
+        const cplx<T> u = x[c];
+        const double f = inv * fr;
+        const int s2 = c / Dr, cc = c - s2 * Dr;
+        D.Ar[((long long)s2 * k + i) * Dr + cc] = mk<T>((T)(u.re * f), (T)(-u.im * f));
+      }
     }
-    if (!D.right_sweep) {
-      const double sn = keep > 0 ? sig / keep : 0.0;
-      u = mk<T>((T)(u.re * sn), (T)(u.im * sn));
-    }
-    // A_l[s1][a][i], r = s1 * Dl + a
-    D.Al[(long long)r * k + i] = u;
   }
-  for (long long e = threadIdx.x; e < (long long)n * k; e += blockDim.x) {
-    const int c = (int)(e % n);
-    const int i = (int)(e / n);
-    const int j = perm[i];
-    const double sig = snorm[j];
-    cplx<T> v;
-    if (!trans) {
-      v = conj(V[(long long)j * nx + c]);
-    } else {
-      const cplx<T> x = X[(long long)j * mx + c];
-      const double f = sig > 0 ? 1.0 / sig : 0.0;
-      v = mk<T>((T)(x.re * f), (T)(-x.im * f));
+  // CTA 0's shared memory (perm, norms, k) is read through DSMEM above: no CTA may
+  // exit before every CTA of the cluster is done with it.
+  cluster.sync();
+}
+
+template <typename T>
+int svd_cluster_plan(int mx, int nx, int* cs, int* cpc, size_t* smem, int* v_smem) {
+  const size_t es = sizeof(cplx<T>);
+  const size_t limit = 200 * 1024;
+  for (int vs = 1; vs >= 0; --vs) {
+    for (int c = 1; c <= 16; c *= 2) {
+      const int per = (nx + c - 1) / c;
+      const size_t bytes = (size_t)per * (mx + (vs ? nx : 0)) * es;
+      if (bytes <= limit) {
+        *cs = c;
+        *cpc = per;
+        *smem = bytes;
+        *v_smem = vs;
+        return QCA_OK;
+      }
     }
-    if (D.right_sweep) {
-      const double sn = keep > 0 ? sig / keep : 0.0;
-      v = mk<T>((T)(v.re * sn), (T)(v.im * sn));
-    }
-    // A_r[s2][i][cc], c = s2 * Dr + cc
-    const int s2 = c / Dr, cc = c - s2 * Dr;
-    D.Ar[((long long)s2 * k + i) * Dr + cc] = v;
   }
+  return QCA_ERR_INVALID;
 }
 
 }  // namespace
 
+// shared-memory footprint check used by the host before choosing this path
 template <typename T>
-int launch_svd(const SvdDesc<T>* d, int nd, cudaStream_t st) {
+bool svd_fits(int Dl, int Dr) {
+  const int m = 2 * Dl, n = 2 * Dr;
+  int cs, cpc, vs;
+  size_t sm;
+  return svd_cluster_plan<T>(m > n ? m : n, m > n ? n : m, &cs, &cpc, &sm, &vs) == QCA_OK;
+}
+
+template <typename T>
+int launch_svd(const SvdDesc<T>* d, const SvdDesc<T>* h, int nd, cudaStream_t st) {
   if (nd <= 0) return QCA_OK;
-  svd_kernel<T><<<nd, kSvdThreads, 0, st>>>(d);
-  QCA_LAUNCH_CHECK();
+  int mxmax = 1, nxmax = 1;
+  for (int i = 0; i < nd; ++i) {
+    const int m = 2 * h[i].Dl, n = 2 * h[i].Dr;
+    mxmax = std::max(mxmax, std::max(m, n));
+    nxmax = std::max(nxmax, std::min(m, n));
+  }
+  int cs = 1, cpc = 1, vs = 1;
+  size_t smem = 0;
+  if (svd_cluster_plan<T>(mxmax, nxmax, &cs, &cpc, &smem, &vs) != QCA_OK) {
+    set_error("SVD of %d x %d exceeds the distributed shared memory of a 16-CTA cluster", mxmax, nxmax);
+    return QCA_ERR_INVALID;
+  }
+  static bool configured[2] = {false, false};
+  const int ti = sizeof(T) == 8 ? 0 : 1;
+  if (!configured[ti]) {
+    QCA_CUDA(cudaFuncSetAttribute(svd_cluster_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    QCA_CUDA(cudaFuncSetAttribute(svd_cluster_kernel<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    configured[ti] = true;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nd * cs, 1, 1);
+  cfg.blockDim = dim3(kSvdThreads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = cs;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  QCA_CUDA(cudaLaunchKernelEx(&cfg, svd_cluster_kernel<T>, d, cs, cpc, vs));
   return QCA_OK;
 }
 
-template int launch_svd<double>(const SvdDesc<double>*, int, cudaStream_t);
-template int launch_svd<float>(const SvdDesc<float>*, int, cudaStream_t);
+template int launch_svd<double>(const SvdDesc<double>*, const SvdDesc<double>*, int, cudaStream_t);
+template int launch_svd<float>(const SvdDesc<float>*, const SvdDesc<float>*, int, cudaStream_t);
+template bool svd_fits<double>(int, int);
+template bool svd_fits<float>(int, int);
 
 }  // namespace qca

@@ -126,7 +126,7 @@ struct SvdDesc {
   int right_sweep;       // 1: A_l = U, A_r = s Vh ; 0: A_l = U s, A_r = Vh
   cplx<T>* Al;           // out (2, Dl, k)
   cplx<T>* Ar;           // out (2, k, Dr)
-  cplx<T>* work;         // m_x * n_x + n_x * n_x elements
+  cplx<T>* work;         // V columns when they do not fit in the cluster's shared memory (n_x^2)
   double* sv;            // singular values (n_x), FP64
   int* k_out;            // new bond dimension
   double* discarded;     // discarded weight accumulator (+= sum of dropped s^2 / sum s^2)
@@ -134,7 +134,7 @@ struct SvdDesc {
 };
 
 template <typename T>
-int launch_svd(const SvdDesc<T>* d, int nd, cudaStream_t st);
+int launch_svd(const SvdDesc<T>* d, const SvdDesc<T>* h, int nd, cudaStream_t st);
 
 // ----------------------------------------------------------------------------------
 // Householder QR with LAPACK's reflector convention (zgeqrf + zungqr):
