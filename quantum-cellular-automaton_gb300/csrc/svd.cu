@@ -27,7 +27,7 @@ namespace qca {
 
 namespace {
 
-constexpr int kSvdThreads = 1024;
+constexpr int kSvdThreads = 512;
 constexpr int kSvdMaxN = 1024;
 constexpr int kSvdMaxSweeps = 30;
 
@@ -42,7 +42,31 @@ struct Prec<float> {
   static constexpr double eps = 1.2e-7;
 };
 
-template <typename T>
+// Rotate columns (a, b) of length len by (c, smq, spq); each lane stages its RPL rows
+// of both columns in registers, so a pair costs one round of (possibly remote) loads.
+template <typename T, int RPL>
+__device__ __forceinline__ void rotate_pair(cplx<T>* a, cplx<T>* b, int len, int lane, T cc, cplx<T> smq,
+                                            cplx<T> spq) {
+  cplx<T> ra[RPL], rb[RPL];
+#pragma unroll
+  for (int r = 0; r < RPL; ++r) {
+    const int i = lane + 32 * r;
+    if (i < len) {
+      ra[r] = a[i];
+      rb[r] = b[i];
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < RPL; ++r) {
+    const int i = lane + 32 * r;
+    if (i < len) {
+      a[i] = cc * ra[r] + smq * rb[r];
+      b[i] = spq * ra[r] + cc * rb[r];
+    }
+  }
+}
+
+template <typename T, int RPL>
 __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<T>* __restrict__ descs, int cs,
                                                                   int cpc, int v_smem) {
   cg::cluster_group cluster = cg::this_cluster();
@@ -111,10 +135,24 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
         cplx<T>* xp = cluster.map_shared_rank(Xloc, p / cpc) + (long long)(p % cpc) * mx;
         cplx<T>* xq = cluster.map_shared_rank(Xloc, q / cpc) + (long long)(q % cpc) * mx;
         // pair Gram entries and the rotation in the working precision T (the
-        // singular values are re-evaluated in FP64 after convergence)
+        // singular values are re-evaluated in FP64 after convergence); both
+        // columns are staged in registers
+        cplx<T> ru[RPL], rv[RPL];
+#pragma unroll
+        for (int r = 0; r < RPL; ++r) {
+          const int i = lane + 32 * r;
+          if (i < mx) {
+            ru[r] = xp[i];
+            rv[r] = xq[i];
+          } else {
+            ru[r] = mk<T>(0, 0);
+            rv[r] = mk<T>(0, 0);
+          }
+        }
         T al = 0, be = 0, gr = 0, gi = 0;
-        for (int i = lane; i < mx; i += 32) {
-          const cplx<T> u = xp[i], v = xq[i];
+#pragma unroll
+        for (int r = 0; r < RPL; ++r) {
+          const cplx<T> u = ru[r], v = rv[r];
           al = fma(u.re, u.re, fma(u.im, u.im, al));
           be = fma(v.re, v.re, fma(v.im, v.im, be));
           gr = fma(u.re, v.re, fma(u.im, v.im, gr));   // conj(u) v
@@ -139,20 +177,19 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
         const T cc = c;
         const cplx<T> smq = mk<T>(-s * er, s * ei);
         const cplx<T> spq = mk<T>(s * er, s * ei);
-        for (int i = lane; i < mx; i += 32) {
-          const cplx<T> u = xp[i], v = xq[i];
-          xp[i] = cc * u + smq * v;
-          xq[i] = spq * u + cc * v;
+#pragma unroll
+        for (int r = 0; r < RPL; ++r) {
+          const int i = lane + 32 * r;
+          if (i < mx) {
+            xp[i] = cc * ru[r] + smq * rv[r];
+            xq[i] = spq * ru[r] + cc * rv[r];
+          }
         }
         cplx<T>* vp = (v_smem ? cluster.map_shared_rank(Xloc, p / cpc) + (long long)cpc * mx
                               : D.work + (long long)(p / cpc) * cpc * nx) + (long long)(p % cpc) * nx;
         cplx<T>* vq = (v_smem ? cluster.map_shared_rank(Xloc, q / cpc) + (long long)cpc * mx
                               : D.work + (long long)(q / cpc) * cpc * nx) + (long long)(q % cpc) * nx;
-        for (int i = lane; i < nx; i += 32) {
-          const cplx<T> u = vp[i], v = vq[i];
-          vp[i] = cc * u + smq * v;
-          vq[i] = spq * u + cc * v;
-        }
+        rotate_pair<T, RPL>(vp, vq, nx, lane, cc, smq, spq);
       }
       cluster.sync();
     }
@@ -304,12 +341,21 @@ int launch_svd(const SvdDesc<T>* d, const SvdDesc<T>* h, int nd, cudaStream_t st
     set_error("SVD of %d x %d exceeds the distributed shared memory of a 16-CTA cluster", mxmax, nxmax);
     return QCA_ERR_INVALID;
   }
-  static bool configured[2] = {false, false};
-  const int ti = sizeof(T) == 8 ? 0 : 1;
-  if (!configured[ti]) {
-    QCA_CUDA(cudaFuncSetAttribute(svd_cluster_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    QCA_CUDA(cudaFuncSetAttribute(svd_cluster_kernel<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    configured[ti] = true;
+  const int rows = (mxmax + 31) / 32;
+  const int rpl = rows <= 2 ? 2 : rows <= 4 ? 4 : rows <= 8 ? 8 : 16;
+  if (rows > 16) {
+    set_error("SVD column length %d exceeds 512", mxmax);
+    return QCA_ERR_INVALID;
+  }
+  void (*kern)(const SvdDesc<T>*, int, int, int) =
+      rpl == 2 ? svd_cluster_kernel<T, 2>
+               : rpl == 4 ? svd_cluster_kernel<T, 4> : rpl == 8 ? svd_cluster_kernel<T, 8> : svd_cluster_kernel<T, 16>;
+  static bool configured[2][5] = {};
+  const int ti = sizeof(T) == 8 ? 0 : 1, ri = rpl == 2 ? 0 : rpl == 4 ? 1 : rpl == 8 ? 2 : 3;
+  if (!configured[ti][ri]) {
+    QCA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    QCA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    configured[ti][ri] = true;
   }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(nd * cs, 1, 1);
@@ -323,7 +369,7 @@ int launch_svd(const SvdDesc<T>* d, const SvdDesc<T>* h, int nd, cudaStream_t st
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  QCA_CUDA(cudaLaunchKernelEx(&cfg, svd_cluster_kernel<T>, d, cs, cpc, vs));
+  QCA_CUDA(cudaLaunchKernelEx(&cfg, kern, d, cs, cpc, vs));
   return QCA_OK;
 }
 
