@@ -29,7 +29,7 @@ namespace {
 
 constexpr int kSvdThreads = 512;
 constexpr int kSvdMaxN = 1024;
-constexpr int kSvdMaxSweeps = 30;
+constexpr int kSvdMaxSweeps = 24;
 
 template <typename T>
 struct Prec;
@@ -79,6 +79,8 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
   __shared__ int s_flag[2];                              // rotation flags (CTA 0), by sweep parity
   __shared__ int s_k;
   __shared__ double s_keep;
+  __shared__ double s_fro;  // ||Theta||_F^2 (CTA 0)
+  __shared__ double red[33];
   const int Dl = D.Dl, Dr = D.Dr;
   const int m = 2 * Dl, n = 2 * Dr;
   const bool trans = n > m;
@@ -107,10 +109,26 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
     }
   }
   if (threadIdx.x < 2) s_flag[threadIdx.x] = 0;
+  if (threadIdx.x == 0) s_fro = 0.0;
   cluster.sync();
+  {
+    // Frobenius norm: columns whose norm is at the rounding floor of the matrix
+    // carry no information; rotating them against large columns only re-injects
+    // rounding noise and would keep the sweeps from terminating.
+    double f = 0.0;
+    for (int lc = 0; lc < cpc; ++lc) {
+      if (rank * cpc + lc >= nx) break;
+      for (int row = threadIdx.x; row < mx; row += blockDim.x) f += (double)norm2(Xloc[(long long)lc * mx + row]);
+    }
+    f = block_sum(f, red);
+    if (threadIdx.x == 0) atomicAdd(cluster.map_shared_rank(&s_fro, 0), f);
+  }
+  cluster.sync();
+  const double fro = *cluster.map_shared_rank(&s_fro, 0);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int P = nx + (nx & 1);
   const double tol = Prec<T>::eps * fmax(8.0, 2.0 * sqrt((double)mx));
+  const T floor2 = (T)(16.0 * Prec<T>::eps * Prec<T>::eps * fro);
   int* flag0 = cluster.map_shared_rank(s_flag, 0);
   int sweep = 0;
   for (; sweep < kSvdMaxSweeps; ++sweep) {
@@ -166,7 +184,7 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
           gi += __shfl_xor_sync(0xffffffffu, gi, o);
         }
         const T g = sqrt(gr * gr + gi * gi);
-        if (!(g > (T)tol * sqrt(al * be))) continue;
+        if (!(g > (T)tol * sqrt(al * be)) || al <= floor2 || be <= floor2) continue;
         rotated = 1;
         const T zeta = (be - al) / (2 * g);
         const T t = (zeta >= 0 ? (T)1 : (T)-1) / (fabs(zeta) + sqrt(1 + zeta * zeta));
