@@ -239,6 +239,7 @@ __global__ void ex_finalize(double* scal) {
     if (k + 1 < m) r += nrm[k + 1];
     rho = fmax(rho, r);
   }
+  if (!isfinite(rho) || fabs(tau) * rho > 1e4) rho = 0.0;  // cannot happen for ||H|| <= n; never loop unbounded
   const int q = max(1, (int)ceil(fabs(tau) * rho / 0.5));
   const double h = tau / q;
   for (int k = lane; k < 64; k += 32) {

@@ -252,6 +252,16 @@ __global__ void lz_finalize_kernel(const LanczosDesc<T>* __restrict__ descs, int
     rho = fmax(rho, r);
   }
   const double tau = D.tau;
+  if (!isfinite(rho) || fabs(tau) * rho > 1e4) {
+    // a non-finite or absurd Krylov matrix: report instead of sub-stepping forever
+    if (lane == 0) {
+      S[LZ_FLAG] = 1.0;
+      S[LZ_MEFF] = (double)m;
+      *done = 1;
+      if (D.done_out) *D.done_out = 1;
+    }
+    return;
+  }
   const int q = max(1, (int)ceil(fabs(tau) * rho / 0.5));
   const double h = tau / q;
   for (int k = lane; k < 64; k += 32) {

@@ -255,6 +255,11 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
       const int cap = D.chi < nx ? D.chi : nx;
       if (k > cap) k = cap;
       if (k > D.kmax) k = D.kmax;
+      // never keep a direction at the rounding floor of the working precision: its
+      // column was not rotated to orthogonality and would break the isometry of
+      // the site tensors (only exact zeros are affected in FP64)
+      const double noise = 4.0 * sqrt((double)floor2);
+      while (k > 1 && snorm[perm[k - 1]] <= noise) --k;
       if (k < 1) k = 1;
       double keep = 0.0;
       for (int i = 0; i < k; ++i) keep += snorm[perm[i]] * snorm[perm[i]];
