@@ -444,17 +444,23 @@ class TDVPOracle:
     # sweeps ------------------------------------------------------------------------
     def step(self) -> None:
         """``tdvp.py:50-63``."""
+        for _ in self.step_updates():
+            pass
+
+    def step_updates(self):
+        """One time step as a generator that yields after every local update
+        (bond update for 2TDVP, site update for 1TDVP), for bounded timing."""
         make_site_canonical(self.A, 0)
         if self.fixed:
             self._refresh_right()
         if self.algorithm == "2tdvp":
-            self._sweep_right_2()
-            self._sweep_left_2()
+            yield from self._sweep_right_2()
+            yield from self._sweep_left_2()
         else:
-            self._sweep_right_1()
-            self._sweep_left_1()
+            yield from self._sweep_right_1()
+            yield from self._sweep_left_1()
 
-    def _sweep_right_2(self) -> None:
+    def _sweep_right_2(self):
         n = len(self.A)
         for site in range(n - 1):
             Al, s, Ar = self._split(self.A[site], self.A[site + 1], self._env("left", site - 1),
@@ -464,8 +470,9 @@ class TDVPOracle:
             if site < n - 2:
                 self._update_env("left", site)
                 self.A[site + 1] = self._evolve_site(site + 1, -self.dt / 2)
+            yield
 
-    def _sweep_left_2(self) -> None:
+    def _sweep_left_2(self):
         n = len(self.A)
         for site in reversed(range(1, n)):
             Al, s, Ar = self._split(self.A[site - 1], self.A[site], self._env("left", site - 2),
@@ -475,8 +482,9 @@ class TDVPOracle:
             if site > 1:
                 self._update_env("right", site)
                 self.A[site - 1] = self._evolve_site(site - 1, -self.dt / 2)
+            yield
 
-    def _sweep_right_1(self) -> None:
+    def _sweep_right_1(self):
         """``tdvp.py:65-84``."""
         n = len(self.A)
         for site in range(n):
@@ -484,6 +492,7 @@ class TDVPOracle:
             new_a = self._evolve_site(site, self.dt / 2)
             if site == n - 1:
                 self.A[site] = new_a
+                yield
                 continue
             q, c = left_qr(new_a, reduced=False)
             self.A[site] = truncate_and_pad(q, tshape)
@@ -491,8 +500,9 @@ class TDVPOracle:
             c = truncate_and_pad(c, (tshape[2], c.shape[1]))
             c = self._evolve_bond(site + 1, c)
             self.A[site + 1] = np.tensordot(c, self.A[site + 1], (1, 1)).transpose(1, 0, 2)
+            yield
 
-    def _sweep_left_1(self) -> None:
+    def _sweep_left_1(self):
         """``tdvp.py:86-105``."""
         n = len(self.A)
         for site in reversed(range(n)):
@@ -500,6 +510,7 @@ class TDVPOracle:
             new_a = self._evolve_site(site, self.dt / 2)
             if site == 0:
                 self.A[site] = new_a
+                yield
                 continue
             q, c = right_qr(new_a, reduced=False)
             self.A[site] = truncate_and_pad(q, tshape)
@@ -507,6 +518,7 @@ class TDVPOracle:
             c = truncate_and_pad(c, (c.shape[0], tshape[1]))
             c = self._evolve_bond(site, c)
             self.A[site - 1] = np.tensordot(self.A[site - 1], c, (2, 0))
+            yield
 
     def measure(self):
         return measure(self.A)
