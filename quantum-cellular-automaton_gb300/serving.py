@@ -1,0 +1,156 @@
+"""Continuous-batching serving loop for TDVP evolution jobs on one GPU.
+
+A job is (rule, N, initial product state, dt, steps, bond cap, algorithm).
+Jobs are admitted as device memory frees up: each chain's footprint comes
+from ``qca_chain_footprint`` (it grows as chi^2 N w) and the sum stays within
+the HBM budget.  Every scheduling round advances every resident job by one
+time step in the same grouped launches (the engine's lock-step ticks), so jobs
+that arrive while others run join the next round and their work overlaps on
+the device.  <n_i> is streamed back every ``stream_every`` steps and at the end
+of each job through ``on_populations(job_id, step, populations)``.
+
+This replaces the reference's per-state driver loop (``quantum_game.py:28-119``:
+one initial state at a time, measure every plot interval) with a multi-job
+server; the per-job arithmetic is the same as a job run alone.
+"""
+from __future__ import annotations
+
+import ctypes
+import time
+from collections import deque
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from .algorithms import _Engine, chain_desc
+from .workloads import ChainSpec, Job
+
+
+@dataclass
+class JobState:
+    job_id: int
+    spec: ChainSpec
+    arrival: float
+    admitted: float = 0.0
+    finished: float = 0.0
+    chain: int = -1
+    steps_done: int = 0
+    bytes: int = 0
+    stream: list = field(default_factory=list)
+
+
+class Server:
+    def __init__(self, precision: str = "mixed", hbm_budget_bytes: int = 150 << 30, stream_every: int = 10,
+                 max_resident: int = 512, on_populations=None) -> None:
+        self.precision = _lib.QCA_PREC_MIXED if precision == "mixed" else _lib.QCA_PREC_FP64
+        self.engine = _Engine(self.precision, hbm_budget_bytes)
+        self.budget = hbm_budget_bytes
+        self.used = 0
+        self.stream_every = stream_every
+        self.max_resident = max_resident
+        self.on_populations = on_populations
+        self.pending: deque[JobState] = deque()
+        self.active: list[JobState] = []
+        self.done: list[JobState] = []
+        self._next_id = 0
+        self.site_updates = 0
+
+    # ------------------------------------------------------------------ requests
+    def submit(self, spec: ChainSpec, arrival: float | None = None) -> int:
+        js = JobState(self._next_id, spec, time.perf_counter() if arrival is None else arrival)
+        self._next_id += 1
+        self.pending.append(js)
+        return js.job_id
+
+    def footprint(self, spec: ChainSpec) -> int:
+        mps = spec.mps()
+        d, keep = chain_desc(mps.A, spec.mpo().W, spec.algorithm, spec.dt, spec.chi, spec.eps)
+        size = ctypes.c_size_t()
+        _lib.call("qca_chain_footprint", ctypes.byref(d), self.precision, ctypes.byref(size))
+        return size.value
+
+    def _admit(self, now: float) -> None:
+        while self.pending and self.pending[0].arrival <= now and len(self.active) < self.max_resident:
+            js = self.pending[0]
+            need = self.footprint(js.spec)
+            if need > self.budget:
+                raise _lib.AdmissionError(_lib.QCA_ERR_ADMISSION, f"job {js.job_id} needs {need} bytes > budget")
+            if self.used + need > self.budget:
+                break  # wait for memory to free up
+            self.pending.popleft()
+            mps = js.spec.mps()
+            d, keep = chain_desc(mps.A, js.spec.mpo().W, js.spec.algorithm, js.spec.dt, js.spec.chi, js.spec.eps)
+            cid = ctypes.c_int(-1)
+            _lib.call("qca_chain_add", self.engine.h, ctypes.byref(d), None, ctypes.byref(cid))
+            js.chain = cid.value
+            js.bytes = need
+            js.admitted = now
+            self.used += need
+            self.active.append(js)
+
+    def _measure(self, jobs: list[JobState]) -> None:
+        if not jobs:
+            return
+        ids = (ctypes.c_int * len(jobs))(*[j.chain for j in jobs])
+        n_tot = sum(j.spec.n for j in jobs)
+        pop = np.zeros(n_tot)
+        _lib.call("qca_engine_measure", self.engine.h, ids, len(jobs), pop.ctypes.data_as(_lib._PD), None, None,
+                  None, None)
+        o = 0
+        for j in jobs:
+            p = pop[o:o + j.spec.n].copy()
+            o += j.spec.n
+            j.stream.append((j.steps_done, p))
+            if self.on_populations:
+                self.on_populations(j.job_id, j.steps_done, p)
+
+    # ------------------------------------------------------------------ loop
+    def round(self, now: float | None = None) -> bool:
+        """Admit what has arrived, advance every resident job by one step,
+        stream populations, retire finished jobs.  Returns False when idle."""
+        now = time.perf_counter() if now is None else now
+        self._admit(now)
+        if not self.active:
+            return bool(self.pending)
+        ids = (ctypes.c_int * len(self.active))(*[j.chain for j in self.active])
+        _lib.call("qca_engine_step_chains", self.engine.h, ids, len(self.active), 1, None)
+        for j in self.active:
+            j.steps_done += 1
+            self.site_updates += j.spec.site_updates_per_step()
+        due = [j for j in self.active if j.steps_done % self.stream_every == 0 or j.steps_done >= j.spec.steps]
+        self._measure(due)
+        t = time.perf_counter()
+        still = []
+        for j in self.active:
+            if j.steps_done >= j.spec.steps:
+                j.finished = t
+                _lib.call("qca_chain_remove", self.engine.h, j.chain)
+                self.used -= j.bytes
+                self.done.append(j)
+            else:
+                still.append(j)
+        self.active = still
+        return True
+
+    def run(self, jobs: list[Job], time_limit: float | None = None) -> dict:
+        """Replay a request trace in real time (arrival offsets in seconds)."""
+        t0 = time.perf_counter()
+        for job in sorted(jobs, key=lambda j: j.arrival):
+            self.submit(job.spec, t0 + job.arrival)
+        while self.pending or self.active:
+            if time_limit is not None and time.perf_counter() - t0 > time_limit:
+                break
+            if not self.active and self.pending and self.pending[0].arrival > time.perf_counter():
+                time.sleep(min(0.01, self.pending[0].arrival - time.perf_counter()))
+            self.round()
+        elapsed = time.perf_counter() - t0
+        return self.report(elapsed)
+
+    def report(self, elapsed: float) -> dict:
+        lat = np.array([j.finished - j.arrival for j in self.done]) if self.done else np.zeros(0)
+        return {"jobs_done": len(self.done), "jobs_pending": len(self.pending), "jobs_active": len(self.active),
+                "site_updates": self.site_updates, "elapsed_s": elapsed,
+                "site_updates_per_s": self.site_updates / elapsed if elapsed > 0 else 0.0,
+                "p50_latency_s": float(np.percentile(lat, 50)) if lat.size else None,
+                "p99_latency_s": float(np.percentile(lat, 99)) if lat.size else None}

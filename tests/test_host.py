@@ -99,3 +99,26 @@ def test_footprint_estimates():
     size = ctypes.c_size_t()
     _lib.call("qca_exact_footprint", 24, _lib.QCA_PREC_FP64, 30, ctypes.byref(size))
     assert size.value >= 30 * 16 * (1 << 24)
+
+
+def test_chain_footprint_grows_with_bond_cap():
+    from qca_gb300.algorithms import chain_desc
+    from qca_gb300 import workloads as W
+    sizes = []
+    for chi in (16, 64, 256):
+        s = W.single_chain(40, 2, range(2, 4), chi, seed=1)
+        mps = s.mps()
+        d, keep = chain_desc(mps.A, s.mpo().W, "2tdvp", 0.05, chi, 1e-10)
+        size = ctypes.c_size_t()
+        _lib.call("qca_chain_footprint", ctypes.byref(d), _lib.QCA_PREC_MIXED, ctypes.byref(size))
+        sizes.append(size.value)
+    assert sizes[0] < sizes[1] < sizes[2]
+    assert sizes[2] > 16 * sizes[0]
+
+
+def test_poisson_trace_shape():
+    from qca_gb300 import workloads as W
+    jobs = W.poisson_jobs(rate=200.0, duration=2.0, seed=3)
+    assert 300 < len(jobs) < 500
+    assert all(12 <= j.spec.n <= 128 and j.spec.distance in (1, 2) for j in jobs)
+    assert all(50 <= j.spec.steps <= 500 for j in jobs)

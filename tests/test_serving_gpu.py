@@ -1,0 +1,62 @@
+"""Serving loop: jobs that arrive while others run are admitted between steps
+and share every launch; each job's streamed populations equal the same job run
+alone (FP64: 1e-12; mixed: 1e-6)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def specs():
+    from qca_gb300 import workloads as W
+    rng = np.random.default_rng(5)
+    out = []
+    for k, (alg, n, d, iv, chi, steps) in enumerate([("2tdvp", 9, 1, range(1, 2), 8, 12), ("1tdvp", 8, 2, range(2, 4), 8, 10),
+                                                    ("2tdvp", 12, 2, range(2, 5), 16, 11), ("2tdvp", 7, 3, range(2, 4), 8, 7),
+                                                    ("1tdvp", 10, 1, range(1, 2), 16, 13)]):
+        out.append(W.ChainSpec(n, d, iv, chi, W.product_probabilities(rng, n), alg, 0.05, 1e-9, steps))
+    return out
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed", 1e-6)])
+def test_each_job_same_alone_and_in_the_mix(precision, tol):
+    from qca_gb300.serving import Server
+    ss = specs()
+    arrivals = [0.0, 0.0, 1.5, 3.0, 3.5]  # virtual arrival times; one round per time unit
+    mix = Server(precision, hbm_budget_bytes=8 << 30, stream_every=5)
+    for s, a in zip(ss, arrivals):
+        mix.submit(s, a)
+    t = 0.0
+    overlap = 0
+    while mix.pending or mix.active:
+        mix.round(now=t)
+        overlap = max(overlap, len(mix.active))
+        t += 1.0
+    assert len(mix.done) == len(ss) and overlap >= 3
+    by_id = {j.job_id: j for j in mix.done}
+    for k, s in enumerate(ss):
+        alone = Server(precision, hbm_budget_bytes=8 << 30, stream_every=5)
+        alone.submit(s, 0.0)
+        while alone.pending or alone.active:
+            alone.round(now=1e9)
+        a = alone.done[0].stream
+        m = by_id[k].stream
+        assert [x[0] for x in a] == [x[0] for x in m]
+        for (sa, pa), (sm, pm) in zip(a, m):
+            assert np.abs(pa - pm).max() < tol, (k, sa)
+
+
+def test_admission_waits_for_memory():
+    from qca_gb300.serving import Server
+    ss = specs()[:3]
+    probe = Server("mixed", hbm_budget_bytes=8 << 30)
+    need = max(probe.footprint(s) for s in ss)
+    srv = Server("mixed", hbm_budget_bytes=int(need * 1.5), stream_every=100)
+    for s in ss:
+        srv.submit(s, 0.0)
+    srv.round(now=0.0)
+    assert len(srv.active) == 1 and len(srv.pending) == 2
+    while srv.pending or srv.active:
+        srv.round(now=1e9)
+        assert srv.used <= srv.budget
+    assert len(srv.done) == 3
