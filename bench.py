@@ -154,6 +154,18 @@ def cuda_events():
     return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
 
+def profiler_region(start: bool) -> None:
+    """Bracket the timed region for ``ncu --profile-from-start off`` when
+    QCA_PROFILE_REGION=1 (no effect otherwise)."""
+    if os.environ.get("QCA_PROFILE_REGION") != "1":
+        return
+    import torch
+    if start:
+        torch.cuda.cudart().cudaProfilerStart()
+    else:
+        torch.cuda.cudart().cudaProfilerStop()
+
+
 # ---------------------------------------------------------------- TDVP workloads
 def build_specs(args, rank: int):
     from qca_gb300 import workloads as W
@@ -240,11 +252,13 @@ def run_tdvp(args, dist: Dist):
     dist.barrier()
     torch.cuda.synchronize()
     clocks.start()
+    profiler_region(True)
     e0, e1 = cuda_events()
     e0.record()
     _lib.call("qca_engine_step_chains", eng.h, cids, len(ids), args.steps, None)
     e1.record()
     torch.cuda.synchronize()
+    profiler_region(False)
     clk = clocks.stop()
     dist.barrier()
     ms = dist.max(e0.elapsed_time(e1))
@@ -345,11 +359,13 @@ def run_exact(args, dist: Dist):
     dist.barrier()
     torch.cuda.synchronize()
     clocks.start()
+    profiler_region(True)
     e0, e1 = cuda_events()
     e0.record()
     a.evolve(args.steps)
     e1.record()
     torch.cuda.synchronize()
+    profiler_region(False)
     clk = clocks.stop()
     ms = dist.max(e0.elapsed_time(e1))
     amps = dist.sum((1 << n) * args.steps)
