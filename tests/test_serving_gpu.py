@@ -50,8 +50,9 @@ def test_admission_waits_for_memory():
     from qca_gb300.serving import Server
     ss = specs()[:3]
     probe = Server("mixed", hbm_budget_bytes=8 << 30)
-    need = max(probe.footprint(s) for s in ss)
-    srv = Server("mixed", hbm_budget_bytes=int(need * 1.5), stream_every=100)
+    f = [probe.footprint(s) for s in ss]
+    # room for the first job, not for the first two together (admission is FIFO)
+    srv = Server("mixed", hbm_budget_bytes=max(f) + f[0] + f[1] - 1 - max(f) + (max(f) - f[0]), stream_every=100)
     for s in ss:
         srv.submit(s, 0.0)
     srv.round(now=0.0)
