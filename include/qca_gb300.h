@@ -83,6 +83,24 @@ int qca_exact_measure(qca_exact* h, double* population, double* rho, void* strea
 /* Bytes of device memory the handle holds. */
 int qca_exact_footprint(int n_cells, int precision, int krylov_dim, size_t* bytes);
 
+/* Allocation-free exact step.  No counterpart in the reference: it exists for
+ * callers that may not allocate device memory (applications whose device memory
+ * is owned by their own pool or budget manager, and latency-critical loops that
+ * cannot take the implicit synchronisation of cudaMalloc / cudaFree).
+ * Evolves the caller's 2^n_cells complex128 amplitudes (DEVICE memory, psi_in and
+ * psi_out may be the same buffer) by nsteps steps of exp(-i pi/2 step_size H) with
+ * the kernels of qca_exact_step, in FP64.  Its scratch (Krylov basis, H v buffer,
+ * Lanczos scalars) is one file-scope device array of 16 MiB that every GPU loading
+ * the library holds until the process exits; it allocates nothing and calls no
+ * allocating routine.  Limit: (krylov_dim + 1) * 2^n_cells * 16 bytes plus a few
+ * KB must fit in 16 MiB (e.g. n_cells <= 15 at krylov_dim 30, <= 14 at 60); larger
+ * requests return QCA_ERR_INVALID.  The first call on a device resolves the
+ * array's device address on that device (make it before any stream capture).
+ * Every call shares the array: calls that overlap on the GPU (other streams,
+ * other host threads) race and must be serialised by the caller. */
+int qca_exact_step_noalloc(int n_cells, int distance, int interval_lo, int interval_hi, int krylov_dim,
+                           double step_size, int nsteps, const void* psi_in, void* psi_out, void* stream);
+
 /* =============================================================================
  * TDVP engine: many MPS chains evolved side by side on one device.
  * Replaces algorithms/tdvp.py:10-365 (TDVP.__init__, do_time_step, the 1-site

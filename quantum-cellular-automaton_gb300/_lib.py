@@ -84,6 +84,7 @@ SIGNATURES = {
     "qca_exact_step": [_P, _D, _I, _P],
     "qca_exact_measure": [_P, _PD, _PD, _P],
     "qca_exact_footprint": [_I, _I, _I, ctypes.POINTER(_SZ)],
+    "qca_exact_step_noalloc": [_I, _I, _I, _I, _I, _D, _I, _P, _P, _P],
     "qca_engine_create": [_I, _SZ, ctypes.POINTER(_P)],
     "qca_engine_destroy": [_P],
     "qca_chain_footprint": [ctypes.POINTER(ChainDesc), _I, ctypes.POINTER(_SZ)],

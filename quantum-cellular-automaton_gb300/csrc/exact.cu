@@ -23,6 +23,7 @@
 // are reduced per block into partials and then by a single-block kernel, so a
 // step is bitwise reproducible.
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -711,3 +712,113 @@ int qca_exact_measure(qca_exact* h, double* population, double* rho, void* strea
 }
 
 }  // extern "C"
+
+// ===================================================================================
+// Allocation-free exact step.
+//
+// Some callers of this library may not allocate device memory at all: host
+// applications whose device memory is owned by their own pool or budget manager,
+// and latency-critical loops that cannot afford the implicit device
+// synchronisation of cudaMalloc / cudaFree.  qca_exact_step_noalloc serves them:
+// it evolves a caller-owned complex128 state (device pointers in and out) with the
+// same kernels as qca_exact_step, but its scratch (the Krylov basis, the H v
+// buffer, the Lanczos scalars and partial sums) lives in the file-scope array
+// below, which every GPU that loads the library holds until the process exits.
+// ===================================================================================
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = 16u << 20;  // 16 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[64] = {};  // per device: device address of g_noalloc_scratch
+
+// Per device, with that device current: resolve the array's device address (the
+// host-side symbol is only a stand-in) and set the kernels' shared-memory limit.
+int noalloc_setup(void** addr) {
+  int dev = 0;
+  QCA_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) {
+    set_error("qca_exact_step_noalloc: device ordinal %d out of range", dev);
+    return QCA_ERR_INVALID;
+  }
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      set_error("qca_exact_step_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+      return QCA_ERR_CUDA;
+    }
+    QCA_TRY(set_smem_attrs<double>());
+    g_noalloc_addr[dev] = p;
+  }
+  *addr = g_noalloc_addr[dev];
+  return QCA_OK;
+}
+
+}  // namespace
+
+extern "C" int qca_exact_step_noalloc(int n_cells, int distance, int interval_lo, int interval_hi, int krylov_dim,
+                                      double step_size, int nsteps, const void* psi_in, void* psi_out,
+                                      void* stream) {
+  if (!psi_in || !psi_out || n_cells < 2 || n_cells > kMaxCells || distance < 1 || interval_lo < 0 ||
+      interval_hi <= interval_lo || krylov_dim < 1 || krylov_dim > 60 || nsteps < 0 || !std::isfinite(step_size)) {
+    set_error("qca_exact_step_noalloc: invalid arguments");
+    return QCA_ERR_INVALID;
+  }
+  ExactImpl E;
+  E.n = n_cells;
+  E.distance = distance;
+  E.lo = interval_lo;
+  E.hi = interval_hi;
+  E.precision = QCA_PREC_FP64;
+  E.m = krylov_dim;
+  E.dim = 1LL << n_cells;
+  E.esize = 16;
+  E.P.n = n_cells;
+  E.P.rule_lo = interval_lo;
+  E.P.rule_hi = interval_hi;
+  E.P.dim = E.dim;
+  for (int b = 0; b < kMaxCells; ++b) E.P.nmask[b] = 0;
+  for (int b = 0; b < n_cells; ++b) {
+    const int i = n_cells - 1 - b;
+    uint32_t mask = 0;
+    for (int jc = std::max(0, i - distance); jc <= std::min(n_cells - 1, i + distance); ++jc)
+      if (jc != i) mask |= 1u << (n_cells - 1 - jc);
+    E.P.nmask[b] = mask;
+  }
+  plan_phases(E);
+  size_t maxtiles = 1;
+  for (auto& g : E.phases) maxtiles = std::max(maxtiles, (size_t)(E.dim >> (g.g + g.kl)));
+  E.partial_count = std::max<size_t>(maxtiles * n_cells * 4, 8 * 152 + 1024);
+  // scratch carve-up: basis (m slots), y, scalars, partials; 256-byte aligned
+  auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+  const size_t b_basis = up(E.esize * E.dim * E.m), b_y = up(E.esize * E.dim);
+  const size_t b_scal = up(sizeof(double) * S_TOTAL), b_part = up(sizeof(double) * E.partial_count);
+  const size_t need = b_basis + b_y + b_scal + b_part;
+  if (need > kNoAllocScratchBytes) {
+    set_error("qca_exact_step_noalloc: %d cells with Krylov dimension %d need %zu bytes of scratch; the static "
+              "scratch holds %zu bytes (use qca_exact_create for larger states)",
+              n_cells, krylov_dim, need, kNoAllocScratchBytes);
+    return QCA_ERR_INVALID;
+  }
+  void* base = nullptr;
+  QCA_TRY(noalloc_setup(&base));
+  char* p = (char*)base;
+  E.basis = p;
+  E.y = p + b_basis;
+  E.scal = (double*)(p + b_basis + b_y);
+  E.partial = (double*)(p + b_basis + b_y + b_scal);
+  cudaStream_t st = (cudaStream_t)stream;
+  // the array keeps the previous call's contents: start from zeroed scalars
+  QCA_CUDA(cudaMemsetAsync(E.scal, 0, b_scal, st));
+  QCA_CUDA(cudaMemcpyAsync(E.basis, psi_in, E.esize * E.dim, cudaMemcpyDeviceToDevice, st));
+  if (nsteps > 0) QCA_TRY(exact_step_impl<double>(E, step_size, nsteps, st));
+  QCA_CUDA(cudaMemcpyAsync(psi_out, E.basis, E.esize * E.dim, cudaMemcpyDeviceToDevice, st));
+  E.basis = nullptr;  // not owned
+  E.y = nullptr;
+  E.scal = nullptr;
+  E.partial = nullptr;
+  return QCA_OK;
+}
