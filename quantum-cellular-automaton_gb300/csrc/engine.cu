@@ -577,9 +577,9 @@ struct Engine final : EngineBase {
         if (s == QCA_OK) s = launch_lz_orth_pass<T>(dd, L.data(), nd, j, 2, st);
         return s;
       }));
-      QCA_TRY(timed(KC_LZFIN, 0, 0, st, [&] { return launch_lz_finalize_j<T>(dd, nd, j, mmax, st); }));
-      QCA_TRY(timed(KC_LZVEC, 0, 0, st, [&] { return launch_lz_normalize<T>(dd, L.data(), nd, j, st); }));
       const bool check = (j >= 3 && (j % 3 == 0)) || j + 1 == mmax;
+      QCA_TRY(timed(KC_LZFIN, 0, 0, st, [&] { return launch_lz_finalize_j<T>(dd, nd, j, mmax, check ? 1 : 0, st); }));
+      QCA_TRY(timed(KC_LZVEC, 0, 0, st, [&] { return launch_lz_normalize<T>(dd, L.data(), nd, j, st); }));
       if (check) {
         QCA_CUDA(cudaMemcpyAsync(h_done, d_done, sizeof(int) * nd, cudaMemcpyDeviceToHost, st));
         QCA_TRY(sync(st));

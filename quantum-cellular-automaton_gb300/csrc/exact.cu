@@ -33,7 +33,7 @@ namespace qca {
 namespace {
 
 constexpr int kMaxCells = 30;
-constexpr int kExactThreads = 1024;
+constexpr int kExactThreads = 512;
 
 struct PhaseGeom {
   int lo;  // first bit of the group
@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(kExactThreads) ex_phase0(ExactParams P, PhaseG
   // u_j = w_j - alpha_{j-1} * v_{j-1}, v_{j-1} = u_{j-1} / ||u_{j-1}||
   T a = 0;
   if (j > 0) a = (T)(scal[S_ALPHA + j - 1] / scal[S_NORM + j - 1]);
-  double nrm = 0.0;
+  T nrm_t = 0;  // per-thread partial in the element precision, summed in FP64 below
   for (int l = threadIdx.x; l < tsize; l += blockDim.x) {
     const long long x = tile_index(G, P.n, t, l);
     cplx<T> u = w[x];
@@ -101,8 +101,9 @@ __global__ void __launch_bounds__(kExactThreads) ex_phase0(ExactParams P, PhaseG
       w[x] = u;
     }
     tile[l] = u;
-    nrm += (double)norm2(u);
+    nrm_t = fma(u.re, u.re, fma(u.im, u.im, nrm_t));
   }
+  double nrm = (double)nrm_t;
   __syncthreads();
   for (int l = threadIdx.x; l < tsize; l += blockDim.x) {
     const long long x = tile_index(G, P.n, t, l);
@@ -124,8 +125,8 @@ __global__ void __launch_bounds__(kExactThreads) ex_phase0(ExactParams P, PhaseG
 
 // Lanczos epilogue for one amplitude: Hv, w_{j+1}, alpha partial.
 template <typename T>
-__device__ __forceinline__ double ex_epilogue_one(cplx<T> hu, cplx<T> u, long long x, cplx<T>* basis, long long dim,
-                                                  int j, bool write_next, T s, T beta_prev, T s_prev) {
+__device__ __forceinline__ T ex_epilogue_one(cplx<T> hu, cplx<T> u, long long x, cplx<T>* basis, long long dim,
+                                             int j, bool write_next, T s, T beta_prev, T s_prev) {
   cplx<T> hv = mk<T>(hu.re * s, hu.im * s);
   const cplx<T> v = mk<T>(u.re * s, u.im * s);
   if (j > 0) {
@@ -135,7 +136,7 @@ __device__ __forceinline__ double ex_epilogue_one(cplx<T> hu, cplx<T> u, long lo
     hv.im = fma(-f, p.im, hv.im);
   }
   if (write_next) basis[(long long)(j + 1) * dim + x] = hv;
-  return (double)(v.re * hv.re + v.im * hv.im);
+  return v.re * hv.re + v.im * hv.im;
 }
 
 // ---------------------------------------------------------------------------------
@@ -157,7 +158,7 @@ __global__ void __launch_bounds__(kExactThreads) ex_phaseH(ExactParams P, PhaseG
   const T beta_prev = j > 0 ? (T)scal[S_NORM + j] : (T)0;
   const T s_prev = j > 0 ? (T)(1.0 / scal[S_NORM + j - 1]) : (T)0;
   const bool write_next = (j + 1) < m;
-  double alpha = 0.0;
+  T alpha_t = 0;
   for (int l = threadIdx.x; l < tsize; l += blockDim.x) {
     const long long x = tile_index(G, P.n, t, l);
     cplx<T> acc = y[x];
@@ -173,11 +174,11 @@ __global__ void __launch_bounds__(kExactThreads) ex_phaseH(ExactParams P, PhaseG
     if (!last) {
       y[x] = acc;
     } else {
-      alpha += ex_epilogue_one(acc, tile[l], x, basis, P.dim, j, write_next, s, beta_prev, s_prev);
+      alpha_t += ex_epilogue_one(acc, tile[l], x, basis, P.dim, j, write_next, s, beta_prev, s_prev);
     }
   }
   if (last) {
-    alpha = block_sum(alpha, red);
+    const double alpha = block_sum((double)alpha_t, red);
     if (threadIdx.x == 0) partial[blockIdx.x] = alpha;
   }
 }
@@ -192,11 +193,11 @@ __global__ void ex_epilogue(ExactParams P, cplx<T>* basis, const cplx<T>* y, dou
   const T beta_prev = j > 0 ? (T)scal[S_NORM + j] : (T)0;
   const T s_prev = j > 0 ? (T)(1.0 / scal[S_NORM + j - 1]) : (T)0;
   const bool write_next = (j + 1) < m;
-  double alpha = 0.0;
+  T alpha_t = 0;
   const cplx<T>* u_j = basis + (long long)j * P.dim;
   for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < P.dim; x += (long long)gridDim.x * blockDim.x)
-    alpha += ex_epilogue_one(y[x], u_j[x], x, basis, P.dim, j, write_next, s, beta_prev, s_prev);
-  alpha = block_sum(alpha, red);
+    alpha_t += ex_epilogue_one(y[x], u_j[x], x, basis, P.dim, j, write_next, s, beta_prev, s_prev);
+  const double alpha = block_sum((double)alpha_t, red);
   if (threadIdx.x == 0) partial[blockIdx.x] = alpha;
 }
 
@@ -437,13 +438,13 @@ namespace {
 
 int plan_phases(ExactImpl& E) {
   // tile capacity: 128 KB of shared memory
-  E.tile_bits = E.precision == QCA_PREC_FP64 ? 13 : 14;
+  E.tile_bits = 13;  // 128 KB (complex128) / 64 KB (complex64) tiles
   E.phases.clear();
   const int g0 = std::min(E.n, E.tile_bits);
   E.phases.push_back(PhaseGeom{0, g0, 0});
   int lo = g0;
   while (lo < E.n) {
-    const int kl_min = E.precision == QCA_PREC_FP64 ? 2 : 3;  // 64-byte runs
+    const int kl_min = 2;  // runs of 4 amplitudes: 64 B (complex128) / 32 B, one sector (complex64)
     int g = std::min(E.n - lo, E.tile_bits - kl_min);
     int kl = std::min(E.tile_bits - g, lo);
     E.phases.push_back(PhaseGeom{lo, g, kl});

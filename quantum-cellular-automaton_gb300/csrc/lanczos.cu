@@ -178,24 +178,24 @@ __global__ void __launch_bounds__(kLzThreads) lz_orth_kernel(const LanczosDesc<T
   }
   double* Pout = P + (long long)(pass & 1) * D.chunks * kPartStride + (long long)ch * kPartStride;
   if (pass < 2) {
-    // projections h_i = <v_i, w> (FP64 products)
+    // projections h_i = <v_i, w>: products and the per-thread partial sum in the
+    // element precision T, the sums across threads and chunks in FP64
     for (int i = 0; i <= j; ++i) {
       const cplx<T>* v = D.V + (long long)i * D.ld;
-      double sr = 0.0, si = 0.0;
+      T tr = 0, ti = 0;
 #pragma unroll
       for (int q = 0; q < kLzPer; ++q) {
         const long long idx = base + q * kLzThreads + threadIdx.x;
         if (idx < D.n) {
           const cplx<T> vv = v[idx];
-          const double ar = vv.re, ai = vv.im, br = r[q].re, bi = r[q].im;
-          sr = fma(ar, br, sr);
-          sr = fma(ai, bi, sr);
-          si = fma(ar, bi, si);
-          si = fma(-ai, br, si);
+          tr = fma(vv.re, r[q].re, tr);
+          tr = fma(vv.im, r[q].im, tr);
+          ti = fma(vv.re, r[q].im, ti);
+          ti = fma(-vv.im, r[q].re, ti);
         }
       }
-      sr = warp_sum(sr);
-      si = warp_sum(si);
+      double sr = warp_sum((double)tr);
+      double si = warp_sum((double)ti);
       if (lane == 0) {
         wsum[wid][2 * i] = sr;
         wsum[wid][2 * i + 1] = si;
@@ -209,10 +209,10 @@ __global__ void __launch_bounds__(kLzThreads) lz_orth_kernel(const LanczosDesc<T
       Pout[i] = s;
     }
   } else {
-    double s = 0.0;
+    T t = 0;
 #pragma unroll
-    for (int q = 0; q < kLzPer; ++q) s += (double)r[q].re * r[q].re + (double)r[q].im * r[q].im;
-    s = warp_sum(s);
+    for (int q = 0; q < kLzPer; ++q) t = fma(r[q].re, r[q].re, fma(r[q].im, r[q].im, t));
+    const double s = warp_sum((double)t);
     if (lane == 0) wsum[wid][0] = s;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(kLzThreads) lz_orth_kernel(const LanczosDesc<T
 
 // One warp per problem: beta_j, exp(-i tau T) e_1, convergence.
 template <typename T>
-__global__ void lz_finalize_kernel(const LanczosDesc<T>* __restrict__ descs, int nd, int j, int mmax) {
+__global__ void lz_finalize_kernel(const LanczosDesc<T>* __restrict__ descs, int nd, int j, int mmax, int check) {
   __shared__ double yr[64], yi[64], tr[64], ti[64], nr[64], ni[64];
   const int di = blockIdx.x;
   const LanczosDesc<T>& D = descs[di];
@@ -242,6 +242,18 @@ __global__ void lz_finalize_kernel(const LanczosDesc<T>* __restrict__ descs, int
   bsq = warp_sum(bsq);
   const double beta = sqrt(bsq);
   const int m = j + 1;  // T is m x m: alpha_0..alpha_j, beta_0..beta_{j-1}
+  if (!check && isfinite(beta) && beta >= S[LZ_TOL] * 1e-3 && m + 1 <= mmax && m + 1 <= kLzMax) {
+    // not a convergence check point: record beta_j and continue without the
+    // tridiagonal exponential (evaluated at check points, breakdown and the end)
+    if (lane == 0) {
+      S[LZ_BETA + j] = beta;
+      S[LZ_MEFF] = (double)m;
+      S[LZ_INVB] = 1.0 / beta;
+      S[LZ_M] = (double)(m + 1);
+      if (D.done_out) *D.done_out = 0;
+    }
+    return;
+  }
   const double* alpha = S + LZ_ALPHA;
   const double* bet = S + LZ_BETA;
   double rho = 0.0;
@@ -262,7 +274,7 @@ __global__ void lz_finalize_kernel(const LanczosDesc<T>* __restrict__ descs, int
     }
     return;
   }
-  const int q = max(1, (int)ceil(fabs(tau) * rho / 0.5));
+  const int q = max(1, (int)ceil(fabs(tau) * rho));
   const double h = tau / q;
   for (int k = lane; k < 64; k += 32) {
     yr[k] = k == 0 ? 1.0 : 0.0;
@@ -469,8 +481,8 @@ int launch_lz_orth_pass(const LanczosDesc<T>* d, const LanczosDesc<T>* h, int nd
 }
 
 template <typename T>
-int launch_lz_finalize_j(const LanczosDesc<T>* d, int nd, int j, int mmax, cudaStream_t st) {
-  lz_finalize_kernel<T><<<nd, 32, 0, st>>>(d, nd, j, mmax);
+int launch_lz_finalize_j(const LanczosDesc<T>* d, int nd, int j, int mmax, int check, cudaStream_t st) {
+  lz_finalize_kernel<T><<<nd, 32, 0, st>>>(d, nd, j, mmax, check);
   QCA_LAUNCH_CHECK();
   return QCA_OK;
 }
@@ -513,7 +525,7 @@ int launch_rho(const cplx<T>* A, int Dl, int Dr, double* rho_out, cudaStream_t s
   template int launch_wapply<T>(const WapplyDesc<T>*, const WapplyDesc<T>*, int, cudaStream_t);                   \
   template int launch_lz_init<T>(const LanczosDesc<T>*, const LanczosDesc<T>*, int, int, double, cudaStream_t);   \
   template int launch_lz_orth_pass<T>(const LanczosDesc<T>*, const LanczosDesc<T>*, int, int, int, cudaStream_t);  \
-  template int launch_lz_finalize_j<T>(const LanczosDesc<T>*, int, int, int, cudaStream_t);                       \
+  template int launch_lz_finalize_j<T>(const LanczosDesc<T>*, int, int, int, int, cudaStream_t);                  \
   template int launch_lz_normalize<T>(const LanczosDesc<T>*, const LanczosDesc<T>*, int, int, cudaStream_t);      \
   template int launch_lz_combine<T>(const LanczosDesc<T>*, const LanczosDesc<T>*, int, cudaStream_t);             \
   template int launch_copy<T>(const CopyDesc<T>*, const CopyDesc<T>*, int, cudaStream_t);                         \

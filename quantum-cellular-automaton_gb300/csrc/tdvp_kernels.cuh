@@ -107,7 +107,7 @@ int launch_lz_init(const LanczosDesc<T>* d, const LanczosDesc<T>* h, int nd, int
 template <typename T>
 int launch_lz_orth_pass(const LanczosDesc<T>* d, const LanczosDesc<T>* h, int nd, int j, int pass, cudaStream_t st);
 template <typename T>
-int launch_lz_finalize_j(const LanczosDesc<T>* d, int nd, int j, int mmax, cudaStream_t st);
+int launch_lz_finalize_j(const LanczosDesc<T>* d, int nd, int j, int mmax, int check, cudaStream_t st);
 template <typename T>
 int launch_lz_normalize(const LanczosDesc<T>* d, const LanczosDesc<T>* h, int nd, int j, cudaStream_t st);
 template <typename T>
