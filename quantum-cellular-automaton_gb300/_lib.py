@@ -99,6 +99,7 @@ SIGNATURES = {
     "qca_chain_stats": [_P, _I, _PD],
     "qca_engine_profile": [_P, _I],
     "qca_engine_kernel_stats": [_P, _PD, _I],
+    "qca_test_gemm_c64": [_I, _I, _I, _P, _P, _P, _I, _P],
 }
 
 _lib = None

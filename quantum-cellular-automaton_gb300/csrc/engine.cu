@@ -211,6 +211,7 @@ struct Engine final : EngineBase {
   std::map<int, std::unique_ptr<Chain<T>>> chains;
   int next_id = 0;
   int mmax = 40;
+  bool use_tc = true;  // tensor-core GEMMs in the mixed path
   double lz_tol = std::is_same<T, double>::value ? 1e-12 : 1e-6;
   // descriptor staging (pinned host + device), bump allocated, reset after a sync
   char* h_stage = nullptr;
@@ -351,7 +352,9 @@ struct Engine final : EngineBase {
       nxx = std::max(nxx, d.N);
     }
     const int cfg = gemm_tile_cfg(mx, nxx);
-    const int td = gemm_tile_dim(cfg);
+    // mixed path: 3xTF32 tensor-core kernel (64 x 64 tiles) unless every problem is tiny
+    const bool tc = std::is_same<T, float>::value && use_tc && cfg >= 1;
+    const int td = tc ? 64 : gemm_tile_dim(cfg);
     int t = 0;
     for (auto& d : v) {
       d.tiles_m = ceil_div(d.M, td);
@@ -367,7 +370,12 @@ struct Engine final : EngineBase {
       fl += 8.0 * d.M * d.N * (double)d.K * nb;
       by += sizeof(cplx<T>) * ((double)d.M * d.K * nb + (double)d.K * d.N * nb + (double)d.M * d.N * d.nb1 * d.nb2);
     }
-    return timed(KC_GEMM, fl, by, st, [&] { return launch_gemm<T>(dd, v.data(), (int)v.size(), cfg, st); });
+    return timed(KC_GEMM, fl, by, st, [&] {
+      if (tc)
+        return launch_gemm_tc(reinterpret_cast<const GemmDesc<float>*>(dd),
+                              reinterpret_cast<const GemmDesc<float>*>(v.data()), (int)v.size(), st);
+      return launch_gemm<T>(dd, v.data(), (int)v.size(), cfg, st);
+    });
   }
 
   int run_wapply(std::vector<WapplyDesc<T>>& v, cudaStream_t st) {

@@ -161,3 +161,240 @@ template int launch_gemm<double>(const GemmDesc<double>*, const GemmDesc<double>
 template int launch_gemm<float>(const GemmDesc<float>*, const GemmDesc<float>*, int, int, cudaStream_t);
 
 }  // namespace qca
+
+// ==================================================================================
+// Tensor-core variant for the mixed path (complex64 operands, FP32 accumulation).
+//
+// Every complex product is four real products and every real product x*y is
+// evaluated as three TF32 products, xh*yh + xh*yl + xl*yh with xh = tf32(x),
+// xl = tf32(x - xh) (the split-precision "3xTF32" scheme), which keeps FP32-level
+// accuracy on the TF32 tensor cores.  The split is done once per element while
+// staging the BM x BK / BK x BN slabs into shared memory (planes re_hi, re_lo,
+// im_hi, im_lo); each warp then issues mma.sync m16n8k8 TF32 on a 32 x 16 warp
+// tile (2 x 2 MMA tiles, 12 MMAs per tile and k8 step).
+// ==================================================================================
+namespace qca {
+
+namespace {
+
+constexpr int kTcBM = 64, kTcBN = 64, kTcBK = 16, kTcPad = 8;
+
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+struct TcSmem {
+  // [plane][k][m or n]; planes: 0 re_hi, 1 re_lo, 2 im_hi, 3 im_lo
+  uint32_t A[4][kTcBK][kTcBM + kTcPad];
+  uint32_t B[4][kTcBK][kTcBN + kTcPad];
+};
+
+__global__ void __launch_bounds__(256) gemm_tc_grouped(const GemmDesc<float>* __restrict__ descs, int nd) {
+  __shared__ TcSmem sm;
+  const int di = find_desc(descs, nd, blockIdx.x);
+  const GemmDesc<float>& D = descs[di];
+  if (D.skip && *D.skip) return;
+  int t = blockIdx.x - D.tile_begin;
+  const int per_batch = D.tiles_m * D.tiles_n;
+  const int b = t / per_batch;
+  t -= b * per_batch;
+  const int b1 = b / D.nb2, b2 = b - b1 * D.nb2;
+  if (b1 >= D.nb1) return;
+  const int tm = t / D.tiles_n, tn = t - tm * D.tiles_n;
+  const int m0 = tm * kTcBM, n0 = tn * kTcBN;
+  const cplx<float>* A = D.A + b1 * D.sAb1 + b2 * D.sAb2;
+  const cplx<float>* B = D.B + b1 * D.sBb1 + b2 * D.sBb2;
+  cplx<float>* C = D.C + b1 * D.sCb1 + b2 * D.sCb2;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int wm = (warp >> 2) * 32;  // warp tile origin in M (2 warps)
+  const int wn = (warp & 3) * 16;   // warp tile origin in N (4 warps)
+  const int g = lane >> 2, tq = lane & 3;
+  float accr[2][2][4], acci[2][2][4];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int r = 0; r < 4; ++r) accr[i][j][r] = acci[i][j][r] = 0.f;
+  const bool a_kfast = D.sAk == 1;
+  const bool b_nfast = D.sBn == 1;
+  for (int gg = 0; gg < D.G; ++gg) {
+    const cplx<float>* Ag = A + gg * D.sAg;
+    const cplx<float>* Bg = B + gg * D.sBg;
+    for (int k0 = 0; k0 < D.K; k0 += kTcBK) {
+      for (int e = threadIdx.x; e < kTcBM * kTcBK; e += 256) {
+        int mm, kk;
+        if (a_kfast) {
+          mm = e / kTcBK;
+          kk = e - mm * kTcBK;
+        } else {
+          kk = e / kTcBM;
+          mm = e - kk * kTcBM;
+        }
+        const int m = m0 + mm, k = k0 + kk;
+        cplx<float> v = mk<float>(0.f, 0.f);
+        if (m < D.M && k < D.K) v = Ag[m * D.sAm + k * D.sAk];
+        if (D.conjA) v.im = -v.im;
+        const uint32_t rh = to_tf32(v.re), ih = to_tf32(v.im);
+        sm.A[0][kk][mm] = rh;
+        sm.A[1][kk][mm] = to_tf32(v.re - __uint_as_float(rh));
+        sm.A[2][kk][mm] = ih;
+        sm.A[3][kk][mm] = to_tf32(v.im - __uint_as_float(ih));
+      }
+      for (int e = threadIdx.x; e < kTcBN * kTcBK; e += 256) {
+        int nn, kk;
+        if (b_nfast) {
+          kk = e / kTcBN;
+          nn = e - kk * kTcBN;
+        } else {
+          nn = e / kTcBK;
+          kk = e - nn * kTcBK;
+        }
+        const int n = n0 + nn, k = k0 + kk;
+        cplx<float> v = mk<float>(0.f, 0.f);
+        if (n < D.N && k < D.K) v = Bg[k * D.sBk + n * D.sBn];
+        if (D.conjB) v.im = -v.im;
+        const uint32_t rh = to_tf32(v.re), ih = to_tf32(v.im);
+        sm.B[0][kk][nn] = rh;
+        sm.B[1][kk][nn] = to_tf32(v.re - __uint_as_float(rh));
+        sm.B[2][kk][nn] = ih;
+        sm.B[3][kk][nn] = to_tf32(v.im - __uint_as_float(ih));
+      }
+      __syncthreads();
+#pragma unroll
+      for (int ks = 0; ks < kTcBK; ks += 8) {
+        uint32_t af[2][4][4];  // [mtile][plane][reg]
+        uint32_t bf[2][4][2];  // [ntile][plane][reg]
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+          const int r0 = wm + 16 * i + g;
+#pragma unroll
+          for (int p = 0; p < 4; ++p) {
+            af[i][p][0] = sm.A[p][ks + tq][r0];
+            af[i][p][1] = sm.A[p][ks + tq][r0 + 8];
+            af[i][p][2] = sm.A[p][ks + tq + 4][r0];
+            af[i][p][3] = sm.A[p][ks + tq + 4][r0 + 8];
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          const int c0 = wn + 8 * j + g;
+#pragma unroll
+          for (int p = 0; p < 4; ++p) {
+            bf[j][p][0] = sm.B[p][ks + tq][c0];
+            bf[j][p][1] = sm.B[p][ks + tq + 4][c0];
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+          uint32_t nih[4], nil[4];  // -Ai (hi, lo): sign flip is exact
+#pragma unroll
+          for (int r = 0; r < 4; ++r) {
+            nih[r] = af[i][2][r] ^ 0x80000000u;
+            nil[r] = af[i][3][r] ^ 0x80000000u;
+          }
+#pragma unroll
+          for (int j = 0; j < 2; ++j) {
+            // small terms first
+            mma_tf32(accr[i][j], af[i][1], bf[j][0]);  // Arl Brh
+            mma_tf32(accr[i][j], af[i][0], bf[j][1]);  // Arh Brl
+            mma_tf32(accr[i][j], nil, bf[j][2]);       // -Ail Bih
+            mma_tf32(accr[i][j], nih, bf[j][3]);       // -Aih Bil
+            mma_tf32(accr[i][j], af[i][0], bf[j][0]);  // Arh Brh
+            mma_tf32(accr[i][j], nih, bf[j][2]);       // -Aih Bih
+            mma_tf32(acci[i][j], af[i][1], bf[j][2]);  // Arl Bih
+            mma_tf32(acci[i][j], af[i][0], bf[j][3]);  // Arh Bil
+            mma_tf32(acci[i][j], af[i][3], bf[j][0]);  // Ail Brh
+            mma_tf32(acci[i][j], af[i][2], bf[j][1]);  // Aih Brl
+            mma_tf32(acci[i][j], af[i][0], bf[j][2]);  // Arh Bih
+            mma_tf32(acci[i][j], af[i][2], bf[j][0]);  // Aih Brh
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const int m = m0 + wm + 16 * i + g + (r >= 2 ? 8 : 0);
+        const int n = n0 + wn + 8 * j + 2 * tq + (r & 1);
+        if (m < D.M && n < D.N) {
+          cplx<float>* c = C + m * D.sCm + n * D.sCn;
+          const cplx<float> v = mk<float>(accr[i][j][r], acci[i][j][r]);
+          *c = D.accumulate ? *c + v : v;
+        }
+      }
+}
+
+}  // namespace
+
+int launch_gemm_tc(const GemmDesc<float>* d_desc, const GemmDesc<float>* h_desc, int ndesc, cudaStream_t st) {
+  if (ndesc <= 0) return QCA_OK;
+  const GemmDesc<float>& last = h_desc[ndesc - 1];
+  const int tiles = last.tile_begin + last.nb1 * last.nb2 * last.tiles_m * last.tiles_n;
+  if (tiles <= 0) return QCA_OK;
+  gemm_tc_grouped<<<tiles, 256, 0, st>>>(d_desc, ndesc);
+  QCA_LAUNCH_CHECK();
+  return QCA_OK;
+}
+
+}  // namespace qca
+
+// Test hook: C = A B for row-major complex64 device matrices through the grouped
+// kernels (tensor_cores: 1 = 3xTF32 tensor-core kernel, 0 = CUDA-core kernel).
+// The single descriptor is passed through a file-scope device slot.
+static __device__ qca::GemmDesc<float> g_test_gemm_slot;
+
+extern "C" int qca_test_gemm_c64(int M, int N, int K, const void* A, const void* B, void* C, int tensor_cores,
+                                 void* stream) {
+  using namespace qca;
+  if (M < 1 || N < 1 || K < 1 || !A || !B || !C) {
+    set_error("qca_test_gemm_c64: invalid arguments");
+    return QCA_ERR_INVALID;
+  }
+  GemmDesc<float> d;
+  memset(&d, 0, sizeof(d));
+  d.A = (const c64*)A;
+  d.B = (const c64*)B;
+  d.C = (c64*)C;
+  d.M = M;
+  d.N = N;
+  d.K = K;
+  d.G = 1;
+  d.nb1 = 1;
+  d.nb2 = 1;
+  d.sAm = K;
+  d.sAk = 1;
+  d.sBk = N;
+  d.sBn = 1;
+  d.sCm = N;
+  d.sCn = 1;
+  const int td = 64;
+  d.tiles_m = ceil_div(M, td);
+  d.tiles_n = ceil_div(N, td);
+  d.tile_begin = 0;
+  GemmDesc<float>* dd = nullptr;
+  cudaStream_t st = (cudaStream_t)stream;
+  void* addr = nullptr;
+  QCA_CUDA(cudaGetSymbolAddress(&addr, g_test_gemm_slot));
+  dd = (GemmDesc<float>*)addr;
+  QCA_CUDA(cudaMemcpyAsync(dd, &d, sizeof(d), cudaMemcpyHostToDevice, st));
+  int s = tensor_cores ? launch_gemm_tc(dd, &d, 1, st) : launch_gemm<float>(dd, &d, 1, 2, st);
+  if (s != QCA_OK) return s;
+  QCA_CUDA(cudaStreamSynchronize(st));
+  return QCA_OK;
+}

@@ -31,6 +31,9 @@ struct GemmDesc {
 template <typename T>
 int launch_gemm(const GemmDesc<T>* d_desc, const GemmDesc<T>* h_desc, int ndesc, int tile_cfg, cudaStream_t st);
 
+// 3xTF32 tensor-core variant (complex64 operands, 64 x 64 tiles).
+int launch_gemm_tc(const GemmDesc<float>* d_desc, const GemmDesc<float>* h_desc, int ndesc, cudaStream_t st);
+
 // Tile configuration for a set of problems (0: 16x16, 1: 32x32, 2: 64x64).
 int gemm_tile_cfg(int maxM, int maxN);
 int gemm_tile_dim(int cfg);
