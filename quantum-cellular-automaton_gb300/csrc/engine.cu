@@ -352,8 +352,9 @@ struct Engine final : EngineBase {
       nxx = std::max(nxx, d.N);
     }
     const int cfg = gemm_tile_cfg(mx, nxx);
-    // mixed path: 3xTF32 tensor-core kernel (64 x 64 tiles) unless every problem is tiny
-    const bool tc = std::is_same<T, float>::value && use_tc && cfg >= 1;
+    // mixed path: always the 3xTF32 tensor-core kernel, so that a chain's arithmetic
+    // does not depend on which other chains share the launch
+    const bool tc = std::is_same<T, float>::value && use_tc;
     const int td = tc ? 64 : gemm_tile_dim(cfg);
     int t = 0;
     for (auto& d : v) {

@@ -1,7 +1,9 @@
 """Numerics of the contraction kernels of the mixed path against a PyTorch
 reference of the same op (complex128 matmul of the same complex64 inputs).
-Tolerance: relative Frobenius error <= 2e-6 (FP32-level; the 3xTF32 split keeps
-the tensor-core kernel at FP32 accuracy)."""
+Tolerance: relative Frobenius error <= 1e-5.  The CUDA-core kernel is FP32
+(about sqrt(K) 6e-8); the 3xTF32 split carries about 22 of FP32's 24 mantissa
+bits per product (the lo*lo term is dropped), about sqrt(K) 2.4e-7 (5e-6 at
+K = 512)."""
 import ctypes
 
 import pytest
@@ -23,4 +25,4 @@ def test_gemm_c64_matches_torch(tc, M, N, K):
               ctypes.c_void_p(C.data_ptr()), tc, None)
     ref = A.to(torch.complex128) @ B.to(torch.complex128)
     err = (C.to(torch.complex128) - ref).norm() / ref.norm()
-    assert err.item() < 2e-6, err.item()
+    assert err.item() < 1e-5, err.item()
