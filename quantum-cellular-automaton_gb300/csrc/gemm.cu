@@ -166,12 +166,13 @@ template int launch_gemm<float>(const GemmDesc<float>*, const GemmDesc<float>*, 
 // Tensor-core variant for the mixed path (complex64 operands, FP32 accumulation).
 //
 // Every complex product is four real products and every real product x*y is
-// evaluated as three TF32 products, xh*yh + xh*yl + xl*yh with xh = tf32(x),
-// xl = tf32(x - xh) (the split-precision "3xTF32" scheme), which keeps FP32-level
-// accuracy on the TF32 tensor cores.  The split is done once per element while
+// evaluated from TF32 parts xh = tf32(x), xl = tf32(x - xh) as
+// xh*yh + xh*yl + xl*yh + xl*yl (split precision; the usual 3xTF32 scheme plus
+// the lo*lo term), which keeps the products at FP32 accuracy on the TF32 tensor
+// cores.  The split is done once per element while
 // staging the BM x BK / BK x BN slabs into shared memory (planes re_hi, re_lo,
 // im_hi, im_lo); each warp then issues mma.sync m16n8k8 TF32 on a 32 x 16 warp
-// tile (2 x 2 MMA tiles, 12 MMAs per tile and k8 step).
+// tile (2 x 2 MMA tiles, 16 MMAs per tile and k8 step).
 // ==================================================================================
 namespace qca {
 
@@ -305,7 +306,11 @@ __global__ void __launch_bounds__(256) gemm_tc_grouped(const GemmDesc<float>* __
           }
 #pragma unroll
           for (int j = 0; j < 2; ++j) {
-            // small terms first
+            // small terms first; the lo*lo terms keep the products at FP32 accuracy
+            mma_tf32(accr[i][j], af[i][1], bf[j][1]);  // Arl Brl
+            mma_tf32(accr[i][j], nil, bf[j][3]);       // -Ail Bil
+            mma_tf32(acci[i][j], af[i][1], bf[j][3]);  // Arl Bil
+            mma_tf32(acci[i][j], af[i][3], bf[j][1]);  // Ail Brl
             mma_tf32(accr[i][j], af[i][1], bf[j][0]);  // Arl Brh
             mma_tf32(accr[i][j], af[i][0], bf[j][1]);  // Arh Brl
             mma_tf32(accr[i][j], nil, bf[j][2]);       // -Ail Bih

@@ -1,9 +1,8 @@
 """Numerics of the contraction kernels of the mixed path against a PyTorch
 reference of the same op (complex128 matmul of the same complex64 inputs).
-Tolerance: relative Frobenius error <= 1e-5.  The CUDA-core kernel is FP32
-(about sqrt(K) 6e-8); the 3xTF32 split carries about 22 of FP32's 24 mantissa
-bits per product (the lo*lo term is dropped), about sqrt(K) 2.4e-7 (5e-6 at
-K = 512)."""
+Tolerance: relative Frobenius error <= 3e-6, FP32 level: about sqrt(K) 6e-8 for
+the CUDA-core kernel and for the tensor-core kernel, whose TF32 split keeps all
+four hi/lo cross products."""
 import ctypes
 
 import pytest
@@ -25,4 +24,4 @@ def test_gemm_c64_matches_torch(tc, M, N, K):
               ctypes.c_void_p(C.data_ptr()), tc, None)
     ref = A.to(torch.complex128) @ B.to(torch.complex128)
     err = (C.to(torch.complex128) - ref).norm() / ref.norm()
-    assert err.item() < 1e-5, err.item()
+    assert err.item() < 3e-6, err.item()
