@@ -306,23 +306,31 @@ __global__ void __launch_bounds__(256) gemm_tc_grouped(const GemmDesc<float>* __
           }
 #pragma unroll
           for (int j = 0; j < 2; ++j) {
-            // small terms first; the lo*lo terms keep the products at FP32 accuracy
-            mma_tf32(accr[i][j], af[i][1], bf[j][1]);  // Arl Brl
-            mma_tf32(accr[i][j], nil, bf[j][3]);       // -Ail Bil
-            mma_tf32(acci[i][j], af[i][1], bf[j][3]);  // Arl Bil
-            mma_tf32(acci[i][j], af[i][3], bf[j][1]);  // Ail Brl
-            mma_tf32(accr[i][j], af[i][1], bf[j][0]);  // Arl Brh
-            mma_tf32(accr[i][j], af[i][0], bf[j][1]);  // Arh Brl
-            mma_tf32(accr[i][j], nil, bf[j][2]);       // -Ail Bih
-            mma_tf32(accr[i][j], nih, bf[j][3]);       // -Aih Bil
-            mma_tf32(accr[i][j], af[i][0], bf[j][0]);  // Arh Brh
-            mma_tf32(accr[i][j], nih, bf[j][2]);       // -Aih Bih
-            mma_tf32(acci[i][j], af[i][1], bf[j][2]);  // Arl Bih
-            mma_tf32(acci[i][j], af[i][0], bf[j][3]);  // Arh Bil
-            mma_tf32(acci[i][j], af[i][3], bf[j][0]);  // Ail Brh
-            mma_tf32(acci[i][j], af[i][2], bf[j][1]);  // Aih Brl
-            mma_tf32(acci[i][j], af[i][0], bf[j][2]);  // Arh Bih
-            mma_tf32(acci[i][j], af[i][2], bf[j][0]);  // Aih Brh
+            // The tensor core's internal accumulation does not round to nearest, so
+            // a k8 step accumulates into zeroed registers and is then added to the
+            // running sums with FP32 adds; small terms first.
+            float tr[4] = {0.f, 0.f, 0.f, 0.f}, ti[4] = {0.f, 0.f, 0.f, 0.f};
+            mma_tf32(tr, af[i][1], bf[j][1]);  // Arl Brl
+            mma_tf32(tr, nil, bf[j][3]);       // -Ail Bil
+            mma_tf32(tr, af[i][1], bf[j][0]);  // Arl Brh
+            mma_tf32(tr, af[i][0], bf[j][1]);  // Arh Brl
+            mma_tf32(tr, nil, bf[j][2]);       // -Ail Bih
+            mma_tf32(tr, nih, bf[j][3]);       // -Aih Bil
+            mma_tf32(tr, af[i][0], bf[j][0]);  // Arh Brh
+            mma_tf32(tr, nih, bf[j][2]);       // -Aih Bih
+            mma_tf32(ti, af[i][1], bf[j][3]);  // Arl Bil
+            mma_tf32(ti, af[i][3], bf[j][1]);  // Ail Brl
+            mma_tf32(ti, af[i][1], bf[j][2]);  // Arl Bih
+            mma_tf32(ti, af[i][0], bf[j][3]);  // Arh Bil
+            mma_tf32(ti, af[i][3], bf[j][0]);  // Ail Brh
+            mma_tf32(ti, af[i][2], bf[j][1]);  // Aih Brl
+            mma_tf32(ti, af[i][0], bf[j][2]);  // Arh Bih
+            mma_tf32(ti, af[i][2], bf[j][0]);  // Aih Brh
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+              accr[i][j][r] += tr[r];
+              acci[i][j][r] += ti[r];
+            }
           }
         }
       }
