@@ -129,14 +129,16 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
           ba = (round + pk) % (PB - 1);
           bb = (round - pk + PB - 1) % (PB - 1);
         }
-        if (ba >= NB || bb >= NB) continue;
+        // a block paired with the padding block still orthogonalises its own two
+        // columns (with a single block this is the only work there is)
+        if (ba >= NB && bb >= NB) continue;
         const int col[4] = {2 * ba, 2 * ba + 1, 2 * bb, 2 * bb + 1};
         bool valid[4];
         cplx<T>* xc[4];
         cplx<T>* vc[4];
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
-          valid[c] = col[c] < nx;
+          valid[c] = (c < 2 ? ba : bb) < NB && col[c] < nx;
           const int cc = valid[c] ? col[c] : 0;
           xc[c] = cluster.map_shared_rank(Xloc, cc / cpc) + (long long)(cc % cpc) * mx;
           vc[c] = (v_smem ? cluster.map_shared_rank(Xloc, cc / cpc) + (long long)cpc * mx
