@@ -6,12 +6,9 @@
 // One-sided (Hestenes) Jacobi on the narrower orientation W (mx >= nx):
 // W = Theta when 2 Dr <= 2 Dl, else W = Theta^H.  Its columns are distributed
 // over the shared memory of a thread-block cluster (1..16 CTAs, distributed
-// shared memory).  Columns are grouped in blocks of two; in every round of a
-// round-robin tournament over the blocks each warp orthogonalises the four
-// columns of one block pair (their 4x4 Gram matrix from one warp reduction, a
-// small two-sided Jacobi on it, the accumulated rotation applied to the columns),
-// reading and writing them through DSMEM; the cluster barrier separates the
-// rounds.  The same rotations accumulate V
+// shared memory); in every round of a round-robin tournament each warp rotates
+// one disjoint column pair, reading and writing both columns through DSMEM, and
+// the cluster barrier separates the rounds.  The same rotations accumulate V
 // (nx x nx), kept beside X in distributed shared memory when the cluster has
 // room and in global memory otherwise.  At convergence X = W V has orthogonal
 // columns whose FP64 norms are the singular values; the site tensors are written
@@ -30,7 +27,7 @@ namespace qca {
 
 namespace {
 
-constexpr int kSvdThreads = 256;
+constexpr int kSvdThreads = 512;
 constexpr int kSvdMaxN = 1024;
 constexpr int kSvdMaxSweeps = 24;
 
@@ -44,6 +41,30 @@ template <>
 struct Prec<float> {
   static constexpr double eps = 1.2e-7;
 };
+
+// Rotate columns (a, b) of length len by (c, smq, spq); each lane stages its RPL rows
+// of both columns in registers, so a pair costs one round of (possibly remote) loads.
+template <typename T, int RPL>
+__device__ __forceinline__ void rotate_pair(cplx<T>* a, cplx<T>* b, int len, int lane, T cc, cplx<T> smq,
+                                            cplx<T> spq) {
+  cplx<T> ra[RPL], rb[RPL];
+#pragma unroll
+  for (int r = 0; r < RPL; ++r) {
+    const int i = lane + 32 * r;
+    if (i < len) {
+      ra[r] = a[i];
+      rb[r] = b[i];
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < RPL; ++r) {
+    const int i = lane + 32 * r;
+    if (i < len) {
+      a[i] = cc * ra[r] + smq * rb[r];
+      b[i] = spq * ra[r] + cc * rb[r];
+    }
+  }
+}
 
 template <typename T, int RPL>
 __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<T>* __restrict__ descs, int cs,
@@ -105,8 +126,7 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
   cluster.sync();
   const double fro = *cluster.map_shared_rank(&s_fro, 0);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const int NB = (nx + 1) / 2;        // column blocks
-  const int PB = NB + (NB & 1);       // padded to even for the tournament
+  const int P = nx + (nx & 1);
   const double tol = Prec<T>::eps * fmax(8.0, 2.0 * sqrt((double)mx));
   const T floor2 = (T)(16.0 * Prec<T>::eps * Prec<T>::eps * fro);
   int* flag0 = cluster.map_shared_rank(s_flag, 0);
@@ -114,150 +134,80 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
   for (; sweep < kSvdMaxSweeps; ++sweep) {
     const int par = sweep & 1;
     int rotated = 0;
-    // Blocks of two columns (block k = columns 2k, 2k+1); every round pairs the
-    // blocks by a round-robin tournament, and a warp orthogonalises the four
-    // columns of its block pair: one reduction gives their 4x4 Gram matrix G
-    // (G_pq = x_p^H x_q), a small two-sided Jacobi diagonalises G while
-    // accumulating the unitary R, and X <- X R, V <- V R are applied in registers.
-    for (int round = 0; round < PB - 1; ++round) {
-      for (int pk = rank + cs * wid; pk < PB / 2; pk += cs * nw) {
-        int ba, bb;
+    for (int round = 0; round < P - 1; ++round) {
+      for (int pk = rank + cs * wid; pk < P / 2; pk += cs * nw) {
+        int p, q;
         if (pk == 0) {
-          ba = PB - 1;
-          bb = round;
+          p = P - 1;
+          q = round;
         } else {
-          ba = (round + pk) % (PB - 1);
-          bb = (round - pk + PB - 1) % (PB - 1);
+          p = (round + pk) % (P - 1);
+          q = (round - pk + P - 1) % (P - 1);
         }
-        // a block paired with the padding block still orthogonalises its own two
-        // columns (with a single block this is the only work there is)
-        if (ba >= NB && bb >= NB) continue;
-        const int col[4] = {2 * ba, 2 * ba + 1, 2 * bb, 2 * bb + 1};
-        bool valid[4];
-        cplx<T>* xc[4];
-        cplx<T>* vc[4];
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          valid[c] = (c < 2 ? ba : bb) < NB && col[c] < nx;
-          const int cc = valid[c] ? col[c] : 0;
-          xc[c] = cluster.map_shared_rank(Xloc, cc / cpc) + (long long)(cc % cpc) * mx;
-          vc[c] = (v_smem ? cluster.map_shared_rank(Xloc, cc / cpc) + (long long)cpc * mx
-                          : D.work + (long long)(cc / cpc) * cpc * nx) + (long long)(cc % cpc) * nx;
+        if (p >= nx || q >= nx) continue;
+        if (p > q) {
+          const int t = p;
+          p = q;
+          q = t;
         }
-        cplx<T> rx[4][RPL];
+        cplx<T>* xp = cluster.map_shared_rank(Xloc, p / cpc) + (long long)(p % cpc) * mx;
+        cplx<T>* xq = cluster.map_shared_rank(Xloc, q / cpc) + (long long)(q % cpc) * mx;
+        // pair Gram entries and the rotation in the working precision T (the
+        // singular values are re-evaluated in FP64 after convergence); both
+        // columns are staged in registers
+        cplx<T> ru[RPL], rv[RPL];
 #pragma unroll
         for (int r = 0; r < RPL; ++r) {
           const int i = lane + 32 * r;
-#pragma unroll
-          for (int c = 0; c < 4; ++c) rx[c][r] = (valid[c] && i < mx) ? xc[c][i] : mk<T>(0, 0);
+          if (i < mx) {
+            ru[r] = xp[i];
+            rv[r] = xq[i];
+          } else {
+            ru[r] = mk<T>(0, 0);
+            rv[r] = mk<T>(0, 0);
+          }
         }
-        // Gram: 4 diagonal entries + 6 complex off-diagonal entries
-        T gd[4] = {0, 0, 0, 0}, gr[6] = {0, 0, 0, 0, 0, 0}, gi[6] = {0, 0, 0, 0, 0, 0};
+        T al = 0, be = 0, gr = 0, gi = 0;
 #pragma unroll
         for (int r = 0; r < RPL; ++r) {
-#pragma unroll
-          for (int c = 0; c < 4; ++c) gd[c] = fma(rx[c][r].re, rx[c][r].re, fma(rx[c][r].im, rx[c][r].im, gd[c]));
-          int k = 0;
-#pragma unroll
-          for (int a = 0; a < 4; ++a)
-#pragma unroll
-            for (int b = a + 1; b < 4; ++b, ++k) {
-              const cplx<T> u = rx[a][r], v = rx[b][r];
-              gr[k] = fma(u.re, v.re, fma(u.im, v.im, gr[k]));
-              gi[k] = fma(u.re, v.im, fma(-u.im, v.re, gi[k]));
-            }
+          const cplx<T> u = ru[r], v = rv[r];
+          al = fma(u.re, u.re, fma(u.im, u.im, al));
+          be = fma(v.re, v.re, fma(v.im, v.im, be));
+          gr = fma(u.re, v.re, fma(u.im, v.im, gr));   // conj(u) v
+          gi = fma(u.re, v.im, fma(-u.im, v.re, gi));
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
-#pragma unroll
-          for (int c = 0; c < 4; ++c) gd[c] += __shfl_xor_sync(0xffffffffu, gd[c], o);
-#pragma unroll
-          for (int k = 0; k < 6; ++k) {
-            gr[k] += __shfl_xor_sync(0xffffffffu, gr[k], o);
-            gi[k] += __shfl_xor_sync(0xffffffffu, gi[k], o);
-          }
+          al += __shfl_xor_sync(0xffffffffu, al, o);
+          be += __shfl_xor_sync(0xffffffffu, be, o);
+          gr += __shfl_xor_sync(0xffffffffu, gr, o);
+          gi += __shfl_xor_sync(0xffffffffu, gi, o);
         }
-        cplx<T> G[4][4], R[4][4];
-        {
-          int k = 0;
-#pragma unroll
-          for (int a = 0; a < 4; ++a) {
-            G[a][a] = mk<T>(gd[a], 0);
-#pragma unroll
-            for (int b = 0; b < 4; ++b) R[a][b] = mk<T>(a == b ? (T)1 : (T)0, (T)0);
-#pragma unroll
-            for (int b = a + 1; b < 4; ++b, ++k) {
-              G[a][b] = mk<T>(gr[k], gi[k]);
-              G[b][a] = mk<T>(gr[k], -gi[k]);
-            }
-          }
-        }
-        bool any = false;
-#pragma unroll 1
-        for (int inner = 0; inner < 3; ++inner) {
-#pragma unroll
-          for (int a = 0; a < 4; ++a)
-#pragma unroll
-            for (int b = a + 1; b < 4; ++b) {
-              if (!valid[a] || !valid[b]) continue;
-              const T al = G[a][a].re, be = G[b][b].re;
-              const T g = sqrt(G[a][b].re * G[a][b].re + G[a][b].im * G[a][b].im);
-              if (!(g > (T)tol * sqrt(al * be)) || al <= floor2 || be <= floor2) continue;
-              if (inner == 0) any = true;
-              const T zeta = (be - al) / (2 * g);
-              const T t = (zeta >= 0 ? (T)1 : (T)-1) / (fabs(zeta) + sqrt(1 + zeta * zeta));
-              const T c = 1 / sqrt(1 + t * t);
-              const T s = c * t;
-              const T er = G[a][b].re / g, ei = G[a][b].im / g;  // e^{i phi}
-              const cplx<T> smq = mk<T>(-s * er, s * ei);  // J[b][a]
-              const cplx<T> spq = mk<T>(s * er, s * ei);   // J[a][b]
-              // G <- G J (columns a, b), then G <- J^H G (rows a, b); R <- R J
-#pragma unroll
-              for (int k = 0; k < 4; ++k) {
-                const cplx<T> p = G[k][a], q = G[k][b];
-                G[k][a] = c * p + smq * q;
-                G[k][b] = spq * p + c * q;
-                const cplx<T> rp = R[k][a], rq = R[k][b];
-                R[k][a] = c * rp + smq * rq;
-                R[k][b] = spq * rp + c * rq;
-              }
-#pragma unroll
-              for (int k = 0; k < 4; ++k) {
-                const cplx<T> p = G[a][k], q = G[b][k];
-                G[a][k] = c * p + conj(smq) * q;
-                G[b][k] = conj(spq) * p + c * q;
-              }
-            }
-        }
-        if (!any) continue;
+        const T g = sqrt(gr * gr + gi * gi);
+        if (!(g > (T)tol * sqrt(al * be)) || al <= floor2 || be <= floor2) continue;
         rotated = 1;
-        // X <- X R on this warp's rows (registers), V <- V R
+        const T zeta = (be - al) / (2 * g);
+        const T t = (zeta >= 0 ? (T)1 : (T)-1) / (fabs(zeta) + sqrt(1 + zeta * zeta));
+        const T c = 1 / sqrt(1 + t * t);
+        const T s = c * t;
+        const T er = gr / g, ei = gi / g;  // e^{i phi}
+        // x_p' = c x_p - s e^{-i phi} x_q ; x_q' = s e^{i phi} x_p + c x_q  (unitary)
+        const T cc = c;
+        const cplx<T> smq = mk<T>(-s * er, s * ei);
+        const cplx<T> spq = mk<T>(s * er, s * ei);
 #pragma unroll
         for (int r = 0; r < RPL; ++r) {
           const int i = lane + 32 * r;
-          if (i >= mx) continue;
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            if (!valid[q]) continue;
-            cplx<T> acc = mk<T>(0, 0);
-#pragma unroll
-            for (int p2 = 0; p2 < 4; ++p2) cfma(acc, rx[p2][r], R[p2][q]);
-            xc[q][i] = acc;
+          if (i < mx) {
+            xp[i] = cc * ru[r] + smq * rv[r];
+            xq[i] = spq * ru[r] + cc * rv[r];
           }
         }
-        for (int i = lane; i < nx; i += 32) {
-          cplx<T> rv[4];
-#pragma unroll
-          for (int c = 0; c < 4; ++c) rv[c] = valid[c] ? vc[c][i] : mk<T>(0, 0);
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            if (!valid[q]) continue;
-            cplx<T> acc = mk<T>(0, 0);
-#pragma unroll
-            for (int p2 = 0; p2 < 4; ++p2) cfma(acc, rv[p2], R[p2][q]);
-            vc[q][i] = acc;
-          }
-        }
+        cplx<T>* vp = (v_smem ? cluster.map_shared_rank(Xloc, p / cpc) + (long long)cpc * mx
+                              : D.work + (long long)(p / cpc) * cpc * nx) + (long long)(p % cpc) * nx;
+        cplx<T>* vq = (v_smem ? cluster.map_shared_rank(Xloc, q / cpc) + (long long)cpc * mx
+                              : D.work + (long long)(q / cpc) * cpc * nx) + (long long)(q % cpc) * nx;
+        rotate_pair<T, RPL>(vp, vq, nx, lane, cc, smq, spq);
       }
       cluster.sync();
     }
