@@ -278,6 +278,11 @@ struct Engine final : EngineBase {
 
   ~Engine() override {
     for (auto e : ev_pool) cudaEventDestroy(e);
+    for (int i = 0; i < 4; ++i) {
+      if (aux[i]) cudaStreamDestroy(aux[i]);
+      if (join_ev[i]) cudaEventDestroy(join_ev[i]);
+    }
+    if (fork_ev) cudaEventDestroy(fork_ev);
     for (auto& kv : chains) cudaFree(kv.second->mem);
     cudaFreeHost(h_stage);
     cudaFree(d_stage);
@@ -451,6 +456,59 @@ struct Engine final : EngineBase {
       if (!in_spans<T>(sp, d.Ar, 2LL * d.kmax * d.Dr - 1)) return bad("svd Ar");
       if (nx > 1024) return bad("svd size");
     }
+    return QCA_OK;
+  }
+
+  // SVD problems grouped by the thread-block cluster size they need; the groups run
+  // concurrently on auxiliary streams (fork/join with events), so small problems
+  // are not launched with the cluster size of the largest one.  The order of the
+  // problems does not change any arithmetic.
+  cudaStream_t aux[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t fork_ev = nullptr, join_ev[4] = {nullptr, nullptr, nullptr, nullptr};
+
+  int svd_grouped(std::vector<SvdDesc<T>>& sv, cudaStream_t st) {
+    std::vector<SvdDesc<T>> grp[5];
+    for (auto& d : sv) {
+      const int cs = svd_cluster_size<T>(d.Dl, d.Dr);
+      const int gi = cs <= 1 ? 0 : cs == 2 ? 1 : cs == 4 ? 2 : cs == 8 ? 3 : 4;
+      grp[gi].push_back(d);
+    }
+    int used_groups = 0;
+    for (auto& g : grp) used_groups += !g.empty();
+    if (used_groups <= 1) {
+      const SvdDesc<T>* ds;
+      QCA_TRY(upload(sv, st, &ds));
+      return launch_svd<T>(ds, sv.data(), (int)sv.size(), st);
+    }
+    if (!aux[0]) {
+      for (int i = 0; i < 4; ++i) {
+        QCA_CUDA(cudaStreamCreateWithFlags(&aux[i], cudaStreamNonBlocking));
+        QCA_CUDA(cudaEventCreateWithFlags(&join_ev[i], cudaEventDisableTiming));
+      }
+      QCA_CUDA(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
+    }
+    // descriptors first (stream-ordered copies on st), then fork
+    std::vector<const SvdDesc<T>*> dptr(5, nullptr);
+    for (int g = 0; g < 5; ++g)
+      if (!grp[g].empty()) QCA_TRY(upload(grp[g], st, &dptr[g]));
+    QCA_CUDA(cudaEventRecord(fork_ev, st));
+    int k = 0;
+    std::vector<int> joined;
+    for (int g = 4; g >= 0; --g) {  // largest first
+      if (grp[g].empty()) continue;
+      cudaStream_t s2 = st;
+      if (k < 4) {
+        s2 = aux[k];
+        QCA_CUDA(cudaStreamWaitEvent(s2, fork_ev, 0));
+      }
+      QCA_TRY(launch_svd<T>(dptr[g], grp[g].data(), (int)grp[g].size(), s2));
+      if (s2 != st) {
+        QCA_CUDA(cudaEventRecord(join_ev[k], s2));
+        joined.push_back(k);
+      }
+      ++k;
+    }
+    for (int j : joined) QCA_CUDA(cudaStreamWaitEvent(st, join_ev[j], 0));
     return QCA_OK;
   }
 
@@ -1025,14 +1083,12 @@ struct Engine final : EngineBase {
     }
     if (!sv.empty()) {
       QCA_TRY(check_svd(sv));
-      const SvdDesc<T>* ds;
-      QCA_TRY(upload(sv, st, &ds));
       double fl = 0.0;
       for (auto& d : sv) {  // Golub-Van Loan thin-SVD count, x4 for complex
         const double m = 2.0 * std::max(d.Dl, d.Dr), n = 2.0 * std::min(d.Dl, d.Dr);
         fl += 4.0 * (4.0 * m * m * n + 8.0 * m * n * n + 9.0 * n * n * n);
       }
-      QCA_TRY(timed(KC_SVD, fl, 0, st, [&] { return launch_svd<T>(ds, sv.data(), (int)sv.size(), st); }));
+      QCA_TRY(timed(KC_SVD, fl, 0, st, [&] { return svd_grouped(sv, st); }));
     }
     if (!qr.empty()) {
       QCA_TRY(check_qr(qr));

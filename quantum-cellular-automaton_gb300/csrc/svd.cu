@@ -340,6 +340,16 @@ int svd_cluster_plan(int mx, int nx, int* cs, int* cpc, size_t* smem, int* v_sme
 
 }  // namespace
 
+// cluster size one problem needs (0 if it does not fit); used to group problems
+template <typename T>
+int svd_cluster_size(int Dl, int Dr) {
+  const int m = 2 * Dl, n = 2 * Dr;
+  int cs, cpc, vs;
+  size_t sm;
+  if (svd_cluster_plan<T>(m > n ? m : n, m > n ? n : m, &cs, &cpc, &sm, &vs) != QCA_OK) return 0;
+  return cs;
+}
+
 // shared-memory footprint check used by the host before choosing this path
 template <typename T>
 bool svd_fits(int Dl, int Dr) {
@@ -400,5 +410,7 @@ template int launch_svd<double>(const SvdDesc<double>*, const SvdDesc<double>*, 
 template int launch_svd<float>(const SvdDesc<float>*, const SvdDesc<float>*, int, cudaStream_t);
 template bool svd_fits<double>(int, int);
 template bool svd_fits<float>(int, int);
+template int svd_cluster_size<double>(int, int);
+template int svd_cluster_size<float>(int, int);
 
 }  // namespace qca
