@@ -42,30 +42,6 @@ struct Prec<float> {
   static constexpr double eps = 1.2e-7;
 };
 
-// Rotate columns (a, b) of length len by (c, smq, spq); each lane stages its RPL rows
-// of both columns in registers, so a pair costs one round of (possibly remote) loads.
-template <typename T, int RPL>
-__device__ __forceinline__ void rotate_pair(cplx<T>* a, cplx<T>* b, int len, int lane, T cc, cplx<T> smq,
-                                            cplx<T> spq) {
-  cplx<T> ra[RPL], rb[RPL];
-#pragma unroll
-  for (int r = 0; r < RPL; ++r) {
-    const int i = lane + 32 * r;
-    if (i < len) {
-      ra[r] = a[i];
-      rb[r] = b[i];
-    }
-  }
-#pragma unroll
-  for (int r = 0; r < RPL; ++r) {
-    const int i = lane + 32 * r;
-    if (i < len) {
-      a[i] = cc * ra[r] + smq * rb[r];
-      b[i] = spq * ra[r] + cc * rb[r];
-    }
-  }
-}
-
 template <typename T, int RPL>
 __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<T>* __restrict__ descs, int cs,
                                                                   int cpc, int v_smem) {
@@ -152,20 +128,21 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
         }
         cplx<T>* xp = cluster.map_shared_rank(Xloc, p / cpc) + (long long)(p % cpc) * mx;
         cplx<T>* xq = cluster.map_shared_rank(Xloc, q / cpc) + (long long)(q % cpc) * mx;
-        // pair Gram entries and the rotation in the working precision T (the
-        // singular values are re-evaluated in FP64 after convergence); both
-        // columns are staged in registers
-        cplx<T> ru[RPL], rv[RPL];
+        cplx<T>* vp = (v_smem ? cluster.map_shared_rank(Xloc, p / cpc) + (long long)cpc * mx
+                              : D.work + (long long)(p / cpc) * cpc * nx) + (long long)(p % cpc) * nx;
+        cplx<T>* vq = (v_smem ? cluster.map_shared_rank(Xloc, q / cpc) + (long long)cpc * mx
+                              : D.work + (long long)(q / cpc) * cpc * nx) + (long long)(q % cpc) * nx;
+        // both columns of X and of V staged in registers in one round of (possibly
+        // remote) loads; the Gram entries and the rotation in the working precision T
+        // (the singular values are re-evaluated in FP64 after convergence)
+        cplx<T> ru[RPL], rv[RPL], wu[RPL], wv[RPL];
 #pragma unroll
         for (int r = 0; r < RPL; ++r) {
           const int i = lane + 32 * r;
-          if (i < mx) {
-            ru[r] = xp[i];
-            rv[r] = xq[i];
-          } else {
-            ru[r] = mk<T>(0, 0);
-            rv[r] = mk<T>(0, 0);
-          }
+          ru[r] = i < mx ? xp[i] : mk<T>(0, 0);
+          rv[r] = i < mx ? xq[i] : mk<T>(0, 0);
+          wu[r] = i < nx ? vp[i] : mk<T>(0, 0);
+          wv[r] = i < nx ? vq[i] : mk<T>(0, 0);
         }
         T al = 0, be = 0, gr = 0, gi = 0;
 #pragma unroll
@@ -202,12 +179,11 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
             xp[i] = cc * ru[r] + smq * rv[r];
             xq[i] = spq * ru[r] + cc * rv[r];
           }
+          if (i < nx) {
+            vp[i] = cc * wu[r] + smq * wv[r];
+            vq[i] = spq * wu[r] + cc * wv[r];
+          }
         }
-        cplx<T>* vp = (v_smem ? cluster.map_shared_rank(Xloc, p / cpc) + (long long)cpc * mx
-                              : D.work + (long long)(p / cpc) * cpc * nx) + (long long)(p % cpc) * nx;
-        cplx<T>* vq = (v_smem ? cluster.map_shared_rank(Xloc, q / cpc) + (long long)cpc * mx
-                              : D.work + (long long)(q / cpc) * cpc * nx) + (long long)(q % cpc) * nx;
-        rotate_pair<T, RPL>(vp, vq, nx, lane, cc, smq, spq);
       }
       cluster.sync();
     }
@@ -268,7 +244,10 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
       *D.k_out = k;
       if (D.discarded) *D.discarded += total > 0 ? (total - keep) / total : 0.0;
       for (int i = 0; i < nx; ++i) D.sv[i] = snorm[perm[i]];
-      if (D.status) *D.status = (sweep >= kSvdMaxSweeps) ? QCA_ERR_NOT_CONVERGED : 0;
+      if (D.status) {
+        D.status[0] = (sweep >= kSvdMaxSweeps) ? QCA_ERR_NOT_CONVERGED : 0;
+        D.status[1] = sweep + 1;  // sweeps used
+      }
     }
   }
   cluster.sync();
@@ -322,11 +301,13 @@ template <typename T>
 int svd_cluster_plan(int mx, int nx, int* cs, int* cpc, size_t* smem, int* v_smem) {
   const size_t es = sizeof(cplx<T>);
   const size_t limit = 200 * 1024;
+  const int pairs = (nx + 1) / 2, warps = kSvdThreads / 32;
   for (int vs = 1; vs >= 0; --vs) {
     for (int c = 1; c <= 16; c *= 2) {
       const int per = (nx + c - 1) / c;
       const size_t bytes = (size_t)per * (mx + (vs ? nx : 0)) * es;
-      if (bytes <= limit) {
+      // enough warps in the cluster for one column pair each per round
+      if (bytes <= limit && (c * warps >= pairs || c == 16)) {
         *cs = c;
         *cpc = per;
         *smem = bytes;

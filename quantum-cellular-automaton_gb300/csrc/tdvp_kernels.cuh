@@ -133,7 +133,7 @@ struct SvdDesc {
   double* sv;            // singular values (n_x), FP64
   int* k_out;            // new bond dimension
   double* discarded;     // discarded weight accumulator (+= sum of dropped s^2 / sum s^2)
-  int* status;           // 0 ok, QCA_ERR_NOT_CONVERGED
+  int* status;           // [0]: 0 ok / QCA_ERR_NOT_CONVERGED, [1]: Jacobi sweeps used
 };
 
 template <typename T>
