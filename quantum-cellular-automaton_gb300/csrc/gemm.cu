@@ -200,8 +200,20 @@ struct TcSmem {
   uint32_t B[4][kTcBK][kTcBN + kTcPad];
 };
 
-__global__ void __launch_bounds__(256) gemm_tc_grouped(const GemmDesc<float>* __restrict__ descs, int nd) {
-  __shared__ TcSmem sm;
+__device__ __forceinline__ void tc_split_store(uint32_t (&pl)[4][kTcBK][kTcBM + kTcPad], int kk, int mm,
+                                               cplx<float> v) {
+  const uint32_t rh = to_tf32(v.re), ih = to_tf32(v.im);
+  pl[0][kk][mm] = rh;
+  pl[1][kk][mm] = to_tf32(v.re - __uint_as_float(rh));
+  pl[2][kk][mm] = ih;
+  pl[3][kk][mm] = to_tf32(v.im - __uint_as_float(ih));
+}
+
+// Double-buffered: while the warps multiply the slab in shared memory, every thread
+// already holds its elements of the next slab in registers (4 of A, 4 of B).
+__global__ void __launch_bounds__(256, 2) gemm_tc_grouped(const GemmDesc<float>* __restrict__ descs, int nd) {
+  extern __shared__ __align__(16) unsigned char tc_smem_raw[];
+  TcSmem* sm = reinterpret_cast<TcSmem*>(tc_smem_raw);  // two stages
   const int di = find_desc(descs, nd, blockIdx.x);
   const GemmDesc<float>& D = descs[di];
   if (D.skip && *D.skip) return;
@@ -229,113 +241,122 @@ __global__ void __launch_bounds__(256) gemm_tc_grouped(const GemmDesc<float>* __
       for (int r = 0; r < 4; ++r) accr[i][j][r] = acci[i][j][r] = 0.f;
   const bool a_kfast = D.sAk == 1;
   const bool b_nfast = D.sBn == 1;
-  for (int gg = 0; gg < D.G; ++gg) {
+  // this thread's 4 A and 4 B element positions within a slab
+  int amm[4], akk[4], bnn[4], bkk[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int e = threadIdx.x + 256 * q;
+    if (a_kfast) {
+      amm[q] = e / kTcBK;
+      akk[q] = e - amm[q] * kTcBK;
+    } else {
+      akk[q] = e / kTcBM;
+      amm[q] = e - akk[q] * kTcBM;
+    }
+    if (b_nfast) {
+      bkk[q] = e / kTcBN;
+      bnn[q] = e - bkk[q] * kTcBN;
+    } else {
+      bnn[q] = e / kTcBK;
+      bkk[q] = e - bnn[q] * kTcBK;
+    }
+  }
+  const int ksl = (D.K + kTcBK - 1) / kTcBK;  // slabs per K group
+  const int nsl = ksl * D.G;
+  cplx<float> ra[4], rb[4];
+  auto fetch = [&](int sl) {
+    const int gg = sl / ksl, k0 = (sl - gg * ksl) * kTcBK;
     const cplx<float>* Ag = A + gg * D.sAg;
     const cplx<float>* Bg = B + gg * D.sBg;
-    for (int k0 = 0; k0 < D.K; k0 += kTcBK) {
-      for (int e = threadIdx.x; e < kTcBM * kTcBK; e += 256) {
-        int mm, kk;
-        if (a_kfast) {
-          mm = e / kTcBK;
-          kk = e - mm * kTcBK;
-        } else {
-          kk = e / kTcBM;
-          mm = e - kk * kTcBM;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int m = m0 + amm[q], k = k0 + akk[q];
+      ra[q] = (m < D.M && k < D.K) ? Ag[m * D.sAm + k * D.sAk] : mk<float>(0.f, 0.f);
+      const int n = n0 + bnn[q], kb = k0 + bkk[q];
+      rb[q] = (n < D.N && kb < D.K) ? Bg[kb * D.sBk + n * D.sBn] : mk<float>(0.f, 0.f);
+    }
+  };
+  auto stash = [&](int buf) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      cplx<float> va = ra[q], vb = rb[q];
+      if (D.conjA) va.im = -va.im;
+      if (D.conjB) vb.im = -vb.im;
+      tc_split_store(sm[buf].A, akk[q], amm[q], va);
+      tc_split_store(sm[buf].B, bkk[q], bnn[q], vb);
+    }
+  };
+  fetch(0);
+  stash(0);
+  __syncthreads();
+  for (int sl = 0; sl < nsl; ++sl) {
+    const int cur = sl & 1;
+    if (sl + 1 < nsl) fetch(sl + 1);  // global loads in flight during the MMAs
+    const TcSmem& S = sm[cur];
+#pragma unroll
+    for (int ks = 0; ks < kTcBK; ks += 8) {
+      uint32_t af[2][4][4];  // [mtile][plane][reg]
+      uint32_t bf[2][4][2];  // [ntile][plane][reg]
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const int r0 = wm + 16 * i + g;
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+          af[i][p][0] = S.A[p][ks + tq][r0];
+          af[i][p][1] = S.A[p][ks + tq][r0 + 8];
+          af[i][p][2] = S.A[p][ks + tq + 4][r0];
+          af[i][p][3] = S.A[p][ks + tq + 4][r0 + 8];
         }
-        const int m = m0 + mm, k = k0 + kk;
-        cplx<float> v = mk<float>(0.f, 0.f);
-        if (m < D.M && k < D.K) v = Ag[m * D.sAm + k * D.sAk];
-        if (D.conjA) v.im = -v.im;
-        const uint32_t rh = to_tf32(v.re), ih = to_tf32(v.im);
-        sm.A[0][kk][mm] = rh;
-        sm.A[1][kk][mm] = to_tf32(v.re - __uint_as_float(rh));
-        sm.A[2][kk][mm] = ih;
-        sm.A[3][kk][mm] = to_tf32(v.im - __uint_as_float(ih));
       }
-      for (int e = threadIdx.x; e < kTcBN * kTcBK; e += 256) {
-        int nn, kk;
-        if (b_nfast) {
-          kk = e / kTcBN;
-          nn = e - kk * kTcBN;
-        } else {
-          nn = e / kTcBK;
-          kk = e - nn * kTcBK;
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const int c0 = wn + 8 * j + g;
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+          bf[j][p][0] = S.B[p][ks + tq][c0];
+          bf[j][p][1] = S.B[p][ks + tq + 4][c0];
         }
-        const int n = n0 + nn, k = k0 + kk;
-        cplx<float> v = mk<float>(0.f, 0.f);
-        if (n < D.N && k < D.K) v = Bg[k * D.sBk + n * D.sBn];
-        if (D.conjB) v.im = -v.im;
-        const uint32_t rh = to_tf32(v.re), ih = to_tf32(v.im);
-        sm.B[0][kk][nn] = rh;
-        sm.B[1][kk][nn] = to_tf32(v.re - __uint_as_float(rh));
-        sm.B[2][kk][nn] = ih;
-        sm.B[3][kk][nn] = to_tf32(v.im - __uint_as_float(ih));
       }
-      __syncthreads();
 #pragma unroll
-      for (int ks = 0; ks < kTcBK; ks += 8) {
-        uint32_t af[2][4][4];  // [mtile][plane][reg]
-        uint32_t bf[2][4][2];  // [ntile][plane][reg]
+      for (int i = 0; i < 2; ++i) {
+        uint32_t nih[4], nil[4];  // -Ai (hi, lo): sign flip is exact
 #pragma unroll
-        for (int i = 0; i < 2; ++i) {
-          const int r0 = wm + 16 * i + g;
-#pragma unroll
-          for (int p = 0; p < 4; ++p) {
-            af[i][p][0] = sm.A[p][ks + tq][r0];
-            af[i][p][1] = sm.A[p][ks + tq][r0 + 8];
-            af[i][p][2] = sm.A[p][ks + tq + 4][r0];
-            af[i][p][3] = sm.A[p][ks + tq + 4][r0 + 8];
-          }
+        for (int r = 0; r < 4; ++r) {
+          nih[r] = af[i][2][r] ^ 0x80000000u;
+          nil[r] = af[i][3][r] ^ 0x80000000u;
         }
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
-          const int c0 = wn + 8 * j + g;
-#pragma unroll
-          for (int p = 0; p < 4; ++p) {
-            bf[j][p][0] = sm.B[p][ks + tq][c0];
-            bf[j][p][1] = sm.B[p][ks + tq + 4][c0];
-          }
-        }
-#pragma unroll
-        for (int i = 0; i < 2; ++i) {
-          uint32_t nih[4], nil[4];  // -Ai (hi, lo): sign flip is exact
+          // The tensor core's internal accumulation does not round to nearest, so
+          // a k8 step accumulates into zeroed registers and is then added to the
+          // running sums with FP32 adds; small terms first.
+          float tr[4] = {0.f, 0.f, 0.f, 0.f}, ti[4] = {0.f, 0.f, 0.f, 0.f};
+          mma_tf32(tr, af[i][1], bf[j][1]);  // Arl Brl
+          mma_tf32(tr, nil, bf[j][3]);       // -Ail Bil
+          mma_tf32(tr, af[i][1], bf[j][0]);  // Arl Brh
+          mma_tf32(tr, af[i][0], bf[j][1]);  // Arh Brl
+          mma_tf32(tr, nil, bf[j][2]);       // -Ail Bih
+          mma_tf32(tr, nih, bf[j][3]);       // -Aih Bil
+          mma_tf32(tr, af[i][0], bf[j][0]);  // Arh Brh
+          mma_tf32(tr, nih, bf[j][2]);       // -Aih Bih
+          mma_tf32(ti, af[i][1], bf[j][3]);  // Arl Bil
+          mma_tf32(ti, af[i][3], bf[j][1]);  // Ail Brl
+          mma_tf32(ti, af[i][1], bf[j][2]);  // Arl Bih
+          mma_tf32(ti, af[i][0], bf[j][3]);  // Arh Bil
+          mma_tf32(ti, af[i][3], bf[j][0]);  // Ail Brh
+          mma_tf32(ti, af[i][2], bf[j][1]);  // Aih Brl
+          mma_tf32(ti, af[i][0], bf[j][2]);  // Arh Bih
+          mma_tf32(ti, af[i][2], bf[j][0]);  // Aih Brh
 #pragma unroll
           for (int r = 0; r < 4; ++r) {
-            nih[r] = af[i][2][r] ^ 0x80000000u;
-            nil[r] = af[i][3][r] ^ 0x80000000u;
-          }
-#pragma unroll
-          for (int j = 0; j < 2; ++j) {
-            // The tensor core's internal accumulation does not round to nearest, so
-            // a k8 step accumulates into zeroed registers and is then added to the
-            // running sums with FP32 adds; small terms first.
-            float tr[4] = {0.f, 0.f, 0.f, 0.f}, ti[4] = {0.f, 0.f, 0.f, 0.f};
-            mma_tf32(tr, af[i][1], bf[j][1]);  // Arl Brl
-            mma_tf32(tr, nil, bf[j][3]);       // -Ail Bil
-            mma_tf32(tr, af[i][1], bf[j][0]);  // Arl Brh
-            mma_tf32(tr, af[i][0], bf[j][1]);  // Arh Brl
-            mma_tf32(tr, nil, bf[j][2]);       // -Ail Bih
-            mma_tf32(tr, nih, bf[j][3]);       // -Aih Bil
-            mma_tf32(tr, af[i][0], bf[j][0]);  // Arh Brh
-            mma_tf32(tr, nih, bf[j][2]);       // -Aih Bih
-            mma_tf32(ti, af[i][1], bf[j][3]);  // Arl Bil
-            mma_tf32(ti, af[i][3], bf[j][1]);  // Ail Brl
-            mma_tf32(ti, af[i][1], bf[j][2]);  // Arl Bih
-            mma_tf32(ti, af[i][0], bf[j][3]);  // Arh Bil
-            mma_tf32(ti, af[i][3], bf[j][0]);  // Ail Brh
-            mma_tf32(ti, af[i][2], bf[j][1]);  // Aih Brl
-            mma_tf32(ti, af[i][0], bf[j][2]);  // Arh Bih
-            mma_tf32(ti, af[i][2], bf[j][0]);  // Aih Brh
-#pragma unroll
-            for (int r = 0; r < 4; ++r) {
-              accr[i][j][r] += tr[r];
-              acci[i][j][r] += ti[r];
-            }
+            accr[i][j][r] += tr[r];
+            acci[i][j][r] += ti[r];
           }
         }
       }
-      __syncthreads();
     }
+    if (sl + 1 < nsl) stash(cur ^ 1);  // the other buffer was last read before the previous barrier
+    __syncthreads();
   }
 #pragma unroll
   for (int i = 0; i < 2; ++i)
@@ -360,7 +381,12 @@ int launch_gemm_tc(const GemmDesc<float>* d_desc, const GemmDesc<float>* h_desc,
   const GemmDesc<float>& last = h_desc[ndesc - 1];
   const int tiles = last.tile_begin + last.nb1 * last.nb2 * last.tiles_m * last.tiles_n;
   if (tiles <= 0) return QCA_OK;
-  gemm_tc_grouped<<<tiles, 256, 0, st>>>(d_desc, ndesc);
+  static bool configured = false;
+  if (!configured) {
+    QCA_CUDA(cudaFuncSetAttribute(gemm_tc_grouped, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * sizeof(TcSmem)));
+    configured = true;
+  }
+  gemm_tc_grouped<<<tiles, 256, 2 * sizeof(TcSmem), st>>>(d_desc, ndesc);
   QCA_LAUNCH_CHECK();
   return QCA_OK;
 }
