@@ -42,7 +42,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="batched", choices=["batched", "exact", "single"])
+    ap.add_argument("--workload", default="batched", choices=["batched", "exact", "single", "accuracy", "serving"])
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--chains", type=int, default=256)
     ap.add_argument("--no-e2e", action="store_true")
@@ -464,11 +465,93 @@ def run_reference(args, dist: Dist):
             "e2e": {"value": round(v, 3), "unit": "site-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+# ---------------------------------------------------------------- accuracy and serving
+def run_accuracy(args, dist: Dist):
+    """Mixed precision against the FP64 path (pinned to the oracle at 1e-8) on
+    chains of the batched mix: max |d<n_i>| over every step, discarded weight,
+    bond dimensions, and the site-update rates of both paths on the same chains."""
+    import torch
+    from qca_gb300 import _lib
+    from qca_gb300 import workloads as W
+    from qca_gb300.algorithms import _Engine
+    torch.cuda.set_device(dist.local)
+    specs = [s for s in W.chain_mix(64, seed=1000 + dist.rank) if s.n <= 48][:args.chains if args.chains < 256 else 6]
+    out = {}
+    pops, rates, discs, bonds = {}, {}, {}, {}
+    for name, prec in (("mixed", _lib.QCA_PREC_MIXED), ("fp64", _lib.QCA_PREC_FP64)):
+        eng = _Engine(prec)
+        ids = add_chains(eng, specs, prec)
+        cids = (ctypes.c_int * len(ids))(*ids)
+        n_tot = sum(s.n for s in specs)
+        series = []
+        t_step = 0.0
+        for step in range(args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            _lib.call("qca_engine_step_chains", eng.h, cids, len(ids), 1, None)
+            torch.cuda.synchronize()
+            t_step += time.perf_counter() - t0
+            pop = np.zeros(n_tot)
+            _lib.call("qca_engine_measure", eng.h, cids, len(ids), pop.ctypes.data_as(_lib._PD), None, None, None,
+                      None)
+            series.append(pop)
+        d = 0.0
+        for cid in ids:
+            st = np.zeros(2)
+            _lib.call("qca_chain_stats", eng.h, cid, st.ctypes.data_as(_lib._PD))
+            d = max(d, st[1])
+        bm = 0
+        for cid, s in zip(ids, specs):
+            bb = np.zeros(s.n + 1, dtype=np.int32)
+            _lib.call("qca_chain_bonds", eng.h, cid, bb.ctypes.data_as(_lib._PI))
+            bm = max(bm, int(bb.max()))
+        pops[name], discs[name], bonds[name] = np.array(series), d, bm
+        rates[name] = sum(s.site_updates_per_step() for s in specs) * args.steps / t_step
+        del eng
+    dn = float(np.abs(pops["mixed"] - pops["fp64"]).max())
+    return {"metric": "max|d<n_i>| mixed vs fp64", "value": dn, "unit": "population", "n_gpus": dist.world,
+            "steps": args.steps, "higher_is_better": False, "data": "synthetic",
+            "config": {"workload": f"{len(specs)} chains of the batched mix with N <= 48 "
+                                   f"({[(s.n, s.distance, s.interval.stop - 1, s.chi) for s in specs]})",
+                       "dt": specs[0].dt, "eps": specs[0].eps},
+            "discarded_weight_last_step": {"mixed": discs["mixed"], "fp64": discs["fp64"]},
+            "max_bond_dim": bonds, "site_updates_per_s": {k: round(v, 1) for k, v in rates.items()},
+            "mixed_over_fp64_speedup": round(rates["mixed"] / rates["fp64"], 2)}
+
+
+def run_serving(args, dist: Dist):
+    """The serving configuration replayed in real time for a bounded wall time:
+    Poisson(200/s) arrivals of 1TDVP/2TDVP jobs, N ~ U{12..128}, distance in
+    {1,2}, bond cap in {16,...,256}, 50-500 steps, dt = 0.05, 150 GB budget,
+    <n_i> streamed every 10 steps.  Reports completed jobs, p50/p99 latency,
+    site-updates/s, and the backlog left when the wall time ran out."""
+    import torch
+    from qca_gb300 import workloads as W
+    from qca_gb300.serving import Server
+    torch.cuda.set_device(dist.local)
+    jobs = W.poisson_jobs(rate=200.0, duration=60.0, seed=7 + dist.rank)
+    srv = Server(args.precision, hbm_budget_bytes=150 << 30, stream_every=10)
+    rep = srv.run(jobs, time_limit=args.serve_seconds)
+    return {"metric": "site-updates/s", "value": round(rep["site_updates_per_s"], 1), "unit": "site-updates/s",
+            "n_gpus": dist.world, "higher_is_better": True, "data": "synthetic",
+            "config": {"workload": "serving: Poisson 200/s over 60 s, 1TDVP/2TDVP, N~U{12..128}, d in {1,2}, "
+                                   "chi in {16..256}, 50-500 steps, dt=0.05, HBM budget 150 GB",
+                       "wall_limit_s": args.serve_seconds, "precision": args.precision,
+                       "jobs_in_trace": len(jobs)},
+            "p50_latency_s": rep["p50_latency_s"], "p99_latency_s": rep["p99_latency_s"],
+            "jobs_done": rep["jobs_done"], "jobs_active": rep["jobs_active"], "jobs_pending": rep["jobs_pending"],
+            "elapsed_s": round(rep["elapsed_s"], 1)}
+
+
 def main():
     args = parse()
     dist = Dist(args.gpus)
     if args.impl == "reference":
         line = run_reference(args, dist)
+    elif args.workload == "accuracy":
+        line = run_accuracy(args, dist)
+    elif args.workload == "serving":
+        line = run_serving(args, dist)
     elif args.workload == "exact":
         line = run_exact(args, dist)
     else:
