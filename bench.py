@@ -539,6 +539,8 @@ def run_serving(args, dist: Dist):
                        "wall_limit_s": args.serve_seconds, "precision": args.precision,
                        "jobs_in_trace": len(jobs)},
             "p50_latency_s": rep["p50_latency_s"], "p99_latency_s": rep["p99_latency_s"],
+            "p50_step_round_s": rep["p50_round_s"], "p99_step_round_s": rep["p99_round_s"],
+            "p50_first_populations_s": rep["p50_first_stream_s"], "p99_first_populations_s": rep["p99_first_stream_s"],
             "jobs_done": rep["jobs_done"], "jobs_active": rep["jobs_active"], "jobs_pending": rep["jobs_pending"],
             "elapsed_s": round(rep["elapsed_s"], 1)}
 

@@ -55,6 +55,8 @@ class Server:
         self.done: list[JobState] = []
         self._next_id = 0
         self.site_updates = 0
+        self.round_times: list[float] = []      # wall time of every scheduling round
+        self.first_stream: list[float] = []     # arrival -> first streamed <n_i> per job
 
     # ------------------------------------------------------------------ requests
     def submit(self, spec: ChainSpec, arrival: float | None = None) -> int:
@@ -110,6 +112,7 @@ class Server:
         """Admit what has arrived, advance every resident job by one step,
         stream populations, retire finished jobs.  Returns False when idle."""
         now = time.perf_counter() if now is None else now
+        t_round = time.perf_counter()
         self._admit(now)
         if not self.active:
             return bool(self.pending)
@@ -121,6 +124,10 @@ class Server:
         due = [j for j in self.active if j.steps_done % self.stream_every == 0 or j.steps_done >= j.spec.steps]
         self._measure(due)
         t = time.perf_counter()
+        self.round_times.append(t - t_round)
+        for j in due:
+            if len(j.stream) == 1:
+                self.first_stream.append(t - j.arrival)
         still = []
         for j in self.active:
             if j.steps_done >= j.spec.steps:
@@ -149,8 +156,15 @@ class Server:
 
     def report(self, elapsed: float) -> dict:
         lat = np.array([j.finished - j.arrival for j in self.done]) if self.done else np.zeros(0)
+        rt = np.array(self.round_times) if self.round_times else np.zeros(0)
+        fs = np.array(self.first_stream) if self.first_stream else np.zeros(0)
+
+        def pct(a, q):
+            return float(np.percentile(a, q)) if a.size else None
+
         return {"jobs_done": len(self.done), "jobs_pending": len(self.pending), "jobs_active": len(self.active),
                 "site_updates": self.site_updates, "elapsed_s": elapsed,
                 "site_updates_per_s": self.site_updates / elapsed if elapsed > 0 else 0.0,
-                "p50_latency_s": float(np.percentile(lat, 50)) if lat.size else None,
-                "p99_latency_s": float(np.percentile(lat, 99)) if lat.size else None}
+                "p50_latency_s": pct(lat, 50), "p99_latency_s": pct(lat, 99),
+                "p50_round_s": pct(rt, 50), "p99_round_s": pct(rt, 99),
+                "p50_first_stream_s": pct(fs, 50), "p99_first_stream_s": pct(fs, 99)}
