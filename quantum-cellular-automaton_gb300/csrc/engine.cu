@@ -212,7 +212,10 @@ struct Engine final : EngineBase {
   int next_id = 0;
   int mmax = 40;
   bool use_tc = true;  // tensor-core GEMMs in the mixed path
-  double lz_tol = std::is_same<T, double>::value ? 1e-12 : 1e-6;
+  // Krylov truncation tolerance of every local exponential (error estimate
+  // beta_j |(exp(-i tau T) e_1)_j|).  Thousands of local steps accumulate it, so the
+  // mixed path keeps it well below its 1e-5 population budget.
+  double lz_tol = std::is_same<T, double>::value ? 1e-12 : 1e-9;
   // descriptor staging (pinned host + device), bump allocated, reset after a sync
   char* h_stage = nullptr;
   char* d_stage = nullptr;

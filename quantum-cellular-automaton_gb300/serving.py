@@ -146,11 +146,13 @@ class Server:
         for job in sorted(jobs, key=lambda j: j.arrival):
             self.submit(job.spec, t0 + job.arrival)
         while self.pending or self.active:
-            if time_limit is not None and time.perf_counter() - t0 > time_limit:
+            now = time.perf_counter()
+            if time_limit is not None and now - t0 > time_limit:
                 break
-            if not self.active and self.pending and self.pending[0].arrival > time.perf_counter():
-                time.sleep(min(0.01, self.pending[0].arrival - time.perf_counter()))
-            self.round()
+            if not self.active and self.pending and self.pending[0].arrival > now:
+                time.sleep(min(0.01, self.pending[0].arrival - now))
+            # no admissions that would start after the time limit
+            self.round(now if time_limit is None or now - t0 < time_limit else t0)
         elapsed = time.perf_counter() - t0
         return self.report(elapsed)
 
