@@ -42,6 +42,91 @@ struct Prec<float> {
   static constexpr double eps = 1.2e-7;
 };
 
+// Gram entries of a column pair: ||u||^2, ||v||^2 and u^H v.  In FP32 the sums are
+// compensated (each product split exactly with an FMA, partial sums carried as
+// hi + lo pairs, also through the warp reduction), so that small inner products of
+// nearly orthogonal columns are resolved beyond the sqrt(m) eps32 noise of a plain
+// FP32 sum and the rotations can drive the columns to FP32-level orthogonality.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+struct DF {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    float s, e;
+    two_sum(hi, x, s, e);
+    hi = s;
+    lo += e;
+  }
+  __device__ __forceinline__ void add_prod(float a, float b) {
+    const float p = a * b;
+    const float pe = fmaf(a, b, -p);  // exact product error
+    add(p);
+    lo += pe;
+  }
+  __device__ __forceinline__ void add_df(float h, float l) {
+    float s, e;
+    two_sum(hi, h, s, e);
+    hi = s;
+    lo += e + l;
+  }
+  __device__ __forceinline__ float value() const { return hi + lo; }
+};
+
+template <typename T, int RPL>
+__device__ __forceinline__ void pair_gram(const cplx<T> (&ru)[RPL], const cplx<T> (&rv)[RPL], T& al, T& be, T& gr,
+                                          T& gi) {
+  if constexpr (sizeof(T) == 4) {
+    DF a, b, r, i;
+#pragma unroll
+    for (int k = 0; k < RPL; ++k) {
+      const cplx<T> u = ru[k], v = rv[k];
+      a.add_prod(u.re, u.re);
+      a.add_prod(u.im, u.im);
+      b.add_prod(v.re, v.re);
+      b.add_prod(v.im, v.im);
+      r.add_prod(u.re, v.re);  // conj(u) v
+      r.add_prod(u.im, v.im);
+      i.add_prod(u.re, v.im);
+      i.add_prod(-u.im, v.re);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a.add_df(__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o));
+      b.add_df(__shfl_xor_sync(0xffffffffu, b.hi, o), __shfl_xor_sync(0xffffffffu, b.lo, o));
+      r.add_df(__shfl_xor_sync(0xffffffffu, r.hi, o), __shfl_xor_sync(0xffffffffu, r.lo, o));
+      i.add_df(__shfl_xor_sync(0xffffffffu, i.hi, o), __shfl_xor_sync(0xffffffffu, i.lo, o));
+    }
+    al = a.value();
+    be = b.value();
+    gr = r.value();
+    gi = i.value();
+  } else {
+    T a = 0, b = 0, r = 0, i = 0;
+#pragma unroll
+    for (int k = 0; k < RPL; ++k) {
+      const cplx<T> u = ru[k], v = rv[k];
+      a = fma(u.re, u.re, fma(u.im, u.im, a));
+      b = fma(v.re, v.re, fma(v.im, v.im, b));
+      r = fma(u.re, v.re, fma(u.im, v.im, r));
+      i = fma(u.re, v.im, fma(-u.im, v.re, i));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      b += __shfl_xor_sync(0xffffffffu, b, o);
+      r += __shfl_xor_sync(0xffffffffu, r, o);
+      i += __shfl_xor_sync(0xffffffffu, i, o);
+    }
+    al = a;
+    be = b;
+    gr = r;
+    gi = i;
+  }
+}
+
 template <typename T, int RPL>
 __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<T>* __restrict__ descs, int cs,
                                                                   int cpc, int v_smem) {
@@ -103,7 +188,7 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
   const double fro = *cluster.map_shared_rank(&s_fro, 0);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int P = nx + (nx & 1);
-  const double tol = Prec<T>::eps * fmax(8.0, 2.0 * sqrt((double)mx));
+  const double tol = Prec<T>::eps * (sizeof(T) == 4 ? 8.0 : fmax(8.0, 2.0 * sqrt((double)mx)));
   const T floor2 = (T)(16.0 * Prec<T>::eps * Prec<T>::eps * fro);
   int* flag0 = cluster.map_shared_rank(s_flag, 0);
   int sweep = 0;
@@ -144,22 +229,8 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
           wu[r] = i < nx ? vp[i] : mk<T>(0, 0);
           wv[r] = i < nx ? vq[i] : mk<T>(0, 0);
         }
-        T al = 0, be = 0, gr = 0, gi = 0;
-#pragma unroll
-        for (int r = 0; r < RPL; ++r) {
-          const cplx<T> u = ru[r], v = rv[r];
-          al = fma(u.re, u.re, fma(u.im, u.im, al));
-          be = fma(v.re, v.re, fma(v.im, v.im, be));
-          gr = fma(u.re, v.re, fma(u.im, v.im, gr));   // conj(u) v
-          gi = fma(u.re, v.im, fma(-u.im, v.re, gi));
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          al += __shfl_xor_sync(0xffffffffu, al, o);
-          be += __shfl_xor_sync(0xffffffffu, be, o);
-          gr += __shfl_xor_sync(0xffffffffu, gr, o);
-          gi += __shfl_xor_sync(0xffffffffu, gi, o);
-        }
+        T al, be, gr, gi;
+        pair_gram<T, RPL>(ru, rv, al, be, gr, gi);
         const T g = sqrt(gr * gr + gi * gi);
         if (!(g > (T)tol * sqrt(al * be)) || al <= floor2 || be <= floor2) continue;
         rotated = 1;
