@@ -1347,22 +1347,85 @@ struct Engine final : EngineBase {
     }
     int maxN = 0;
     for (auto* c : C) maxN = std::max(maxN, c->N);
+    // 2TDVP chains whose centre is at site 0 are measured without touching their
+    // tensors: their result does not depend on the gauge, and the left sweep runs
+    // on scratch copies (centre_{s+1} = R_s A[s+1]).  1TDVP chains follow the
+    // reference, whose measurement re-gauges the stored MPS (mps.py:110-117).
+    std::vector<char> keep(C.size(), 0);
+    for (size_t i = 0; i < C.size(); ++i) keep[i] = C[i]->algo == QCA_ALGO_2TDVP && C[i]->center == 0;
+    std::vector<const cplx<T>*> cen(C.size(), nullptr);
+    for (size_t i = 0; i < C.size(); ++i) cen[i] = C[i]->cur(0);
     for (int k = maxN - 1; k >= 1; --k) {
       std::vector<MoveJob> J;
-      for (auto* c : C)
-        if (k < c->N && k <= c->center) J.push_back(MoveJob{c, k, false});
+      for (size_t i = 0; i < C.size(); ++i)
+        if (!keep[i] && k < C[i]->N && k <= C[i]->center) J.push_back(MoveJob{C[i], k, false});
       QCA_TRY(qr_moves(J, st));
     }
     for (int s = 0; s < maxN; ++s) {
       if (s > 0) {
         std::vector<MoveJob> J;
-        for (auto* c : C)
-          if (s < c->N) J.push_back(MoveJob{c, s - 1, true});
+        for (size_t i = 0; i < C.size(); ++i)
+          if (!keep[i] && s < C[i]->N) J.push_back(MoveJob{C[i], s - 1, true});
         QCA_TRY(qr_moves(J, st));
+        // scratch sweep: R of the previous centre times the next site tensor
+        std::vector<QrDesc<T>> q;
+        std::vector<GemmDesc<T>> g;
+        std::vector<size_t> who;
+        for (size_t i = 0; i < C.size(); ++i) {
+          Chain<T>* c = C[i];
+          if (!keep[i] || s >= c->N) continue;
+          const int Dp = c->D[s - 1], Dq = c->D[s], Dn = c->D[s + 1];
+          QrDesc<T> d;
+          memset(&d, 0, sizeof(d));
+          d.in = cen[i];
+          d.rsplit = Dp;
+          d.sIr0 = Dq;
+          d.sIr1 = (long long)Dp * Dq;
+          d.sIc = 1;
+          d.m = 2 * Dp;
+          d.n = Dq;
+          d.work = c->qrw;
+          d.tau = c->qrtau;
+          d.rr = c->cbuf;
+          d.sRr = Dq;
+          d.sRc = 1;
+          d.rrows_out = Dq;
+          d.rcols_out = Dq;
+          q.push_back(d);
+          GemmDesc<T> a = gemm0();
+          a.A = c->cbuf;
+          a.B = c->cur(s);
+          a.C = (s & 1) ? c->theta : c->t1;
+          a.M = Dq;
+          a.K = Dq;
+          a.N = Dn;
+          a.nb1 = 2;
+          a.sAm = Dq;
+          a.sAk = 1;
+          a.sBk = Dn;
+          a.sBn = 1;
+          a.sBb1 = (long long)Dq * Dn;
+          a.sCm = Dn;
+          a.sCn = 1;
+          a.sCb1 = (long long)Dq * Dn;
+          g.push_back(a);
+          who.push_back(i);
+        }
+        if (!q.empty()) {
+          QCA_TRY(check_qr(q));
+          const QrDesc<T>* dq;
+          QCA_TRY(upload(q, st, &dq));
+          QCA_TRY(timed(KC_QR, 0, 0, st, [&] { return launch_qr<T>(dq, (int)q.size(), st); }));
+          QCA_TRY(run_gemm(g, st));
+          for (size_t k = 0; k < who.size(); ++k) cen[who[k]] = g[k].C;
+        }
       }
-      for (auto* c : C)
-        if (s < c->N)
-          QCA_TRY(timed(KC_MISC, 0, 0, st, [&] { return launch_rho<T>(c->cur(s), c->D[s], c->D[s + 1], c->dscal + 8 + 4 * s, st); }));
+      for (size_t i = 0; i < C.size(); ++i) {
+        Chain<T>* c = C[i];
+        if (s >= c->N) continue;
+        const cplx<T>* a = keep[i] ? cen[i] : c->cur(s);
+        QCA_TRY(timed(KC_MISC, 0, 0, st, [&] { return launch_rho<T>(a, c->D[s], c->D[s + 1], c->dscal + 8 + 4 * s, st); }));
+      }
     }
     std::vector<std::vector<double>> rho(C.size());
     for (size_t i = 0; i < C.size(); ++i) {
@@ -1373,7 +1436,7 @@ struct Engine final : EngineBase {
     size_t o = 0;
     for (size_t i = 0; i < C.size(); ++i) {
       Chain<T>* c = C[i];
-      c->center = c->N - 1;
+      if (!keep[i]) c->center = c->N - 1;
       for (int s = 0; s < c->N; ++s) {
         const double* r = rho[i].data() + 4 * s;
         const double r00 = r[0], r11 = r[1], rr = r[2], ri = r[3];
