@@ -56,7 +56,9 @@ enum : int {
   S_NORM = 8,        // S_NORM + j : ||u_j||
   S_ALPHA = 8 + 64,  // S_ALPHA + j: alpha_j
   S_COEF = 8 + 128,  // S_COEF + 2k: complex coefficient of slot k in the combination
-  S_TOTAL = 8 + 128 + 128
+  S_INV = 8 + 256,   // S_INV + j : 1 / ||u_j||
+  S_AOV = 8 + 320,   // S_AOV + j : alpha_j / ||u_j||
+  S_TOTAL = 8 + 384
 };
 
 __device__ __forceinline__ long long tile_index(const PhaseGeom& G, int n, long long t, int l) {
@@ -88,8 +90,7 @@ __global__ void __launch_bounds__(kExactThreads) ex_phase0(ExactParams P, PhaseG
   cplx<T>* w = basis + (long long)j * P.dim;
   const cplx<T>* vp = basis + (long long)(j - 1) * P.dim;
   // u_j = w_j - alpha_{j-1} * v_{j-1}, v_{j-1} = u_{j-1} / ||u_{j-1}||
-  T a = 0;
-  if (j > 0) a = (T)(scal[S_ALPHA + j - 1] / scal[S_NORM + j - 1]);
+  const T a = j > 0 ? (T)scal[S_AOV + j - 1] : (T)0;
   T nrm_t = 0;  // per-thread partial in the element precision, summed in FP64 below
   for (int l = threadIdx.x; l < tsize; l += blockDim.x) {
     const long long x = tile_index(G, P.n, t, l);
@@ -154,9 +155,9 @@ __global__ void __launch_bounds__(kExactThreads) ex_phaseH(ExactParams P, PhaseG
   const cplx<T>* u_j = basis + (long long)j * P.dim;
   for (int l = threadIdx.x; l < tsize; l += blockDim.x) tile[l] = u_j[tile_index(G, P.n, t, l)];
   __syncthreads();
-  const T s = (T)(1.0 / scal[S_NORM + j]);
+  const T s = (T)scal[S_INV + j];
   const T beta_prev = j > 0 ? (T)scal[S_NORM + j] : (T)0;
-  const T s_prev = j > 0 ? (T)(1.0 / scal[S_NORM + j - 1]) : (T)0;
+  const T s_prev = j > 0 ? (T)scal[S_INV + j - 1] : (T)0;
   const bool write_next = (j + 1) < m;
   T alpha_t = 0;
   for (int l = threadIdx.x; l < tsize; l += blockDim.x) {
@@ -189,9 +190,9 @@ __global__ void ex_epilogue(ExactParams P, cplx<T>* basis, const cplx<T>* y, dou
                             int m) {
   if (j >= (int)scal[S_MEFF]) return;
   __shared__ double red[33];
-  const T s = (T)(1.0 / scal[S_NORM + j]);
+  const T s = (T)scal[S_INV + j];
   const T beta_prev = j > 0 ? (T)scal[S_NORM + j] : (T)0;
-  const T s_prev = j > 0 ? (T)(1.0 / scal[S_NORM + j - 1]) : (T)0;
+  const T s_prev = j > 0 ? (T)scal[S_INV + j - 1] : (T)0;
   const bool write_next = (j + 1) < m;
   T alpha_t = 0;
   const cplx<T>* u_j = basis + (long long)j * P.dim;
@@ -219,8 +220,10 @@ __global__ void ex_reduce(double* scal, const double* partial, int count, int ki
       return;
     }
     scal[S_NORM + j] = nrm;
+    scal[S_INV + j] = 1.0 / nrm;
   } else {
     scal[S_ALPHA + j] = v;
+    scal[S_AOV + j] = v / scal[S_NORM + j];
   }
 }
 

@@ -167,12 +167,12 @@ template int launch_gemm<float>(const GemmDesc<float>*, const GemmDesc<float>*, 
 //
 // Every complex product is four real products and every real product x*y is
 // evaluated from TF32 parts xh = tf32(x), xl = tf32(x - xh) as
-// xh*yh + xh*yl + xl*yh + xl*yl (split precision; the usual 3xTF32 scheme plus
-// the lo*lo term), which keeps the products at FP32 accuracy on the TF32 tensor
-// cores.  The split is done once per element while
+// xh*yh + xh*yl + xl*yh (split precision, "3xTF32"); with every k8 step summed
+// into zeroed registers and added to the running sums in FP32, the products keep
+// FP32 accuracy on the TF32 tensor cores.  The split is done once per element while
 // staging the BM x BK / BK x BN slabs into shared memory (planes re_hi, re_lo,
 // im_hi, im_lo); each warp then issues mma.sync m16n8k8 TF32 on a 32 x 16 warp
-// tile (2 x 2 MMA tiles, 16 MMAs per tile and k8 step).
+// tile (2 x 2 MMA tiles, 12 MMAs per tile and k8 step).
 // ==================================================================================
 namespace qca {
 
@@ -331,16 +331,12 @@ __global__ void __launch_bounds__(256, 2) gemm_tc_grouped(const GemmDesc<float>*
           // a k8 step accumulates into zeroed registers and is then added to the
           // running sums with FP32 adds; small terms first.
           float tr[4] = {0.f, 0.f, 0.f, 0.f}, ti[4] = {0.f, 0.f, 0.f, 0.f};
-          mma_tf32(tr, af[i][1], bf[j][1]);  // Arl Brl
-          mma_tf32(tr, nil, bf[j][3]);       // -Ail Bil
           mma_tf32(tr, af[i][1], bf[j][0]);  // Arl Brh
           mma_tf32(tr, af[i][0], bf[j][1]);  // Arh Brl
           mma_tf32(tr, nil, bf[j][2]);       // -Ail Bih
           mma_tf32(tr, nih, bf[j][3]);       // -Aih Bil
           mma_tf32(tr, af[i][0], bf[j][0]);  // Arh Brh
           mma_tf32(tr, nih, bf[j][2]);       // -Aih Bih
-          mma_tf32(ti, af[i][1], bf[j][3]);  // Arl Bil
-          mma_tf32(ti, af[i][3], bf[j][1]);  // Ail Brl
           mma_tf32(ti, af[i][1], bf[j][2]);  // Arl Bih
           mma_tf32(ti, af[i][0], bf[j][3]);  // Arh Bil
           mma_tf32(ti, af[i][3], bf[j][0]);  // Ail Brh

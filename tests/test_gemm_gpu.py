@@ -1,8 +1,8 @@
 """Numerics of the contraction kernels of the mixed path against a PyTorch
 reference of the same op (complex128 matmul of the same complex64 inputs).
 Tolerance: relative Frobenius error <= 3e-6, FP32 level: about sqrt(K) 6e-8 for
-the CUDA-core kernel and for the tensor-core kernel, whose TF32 split keeps all
-four hi/lo cross products."""
+the CUDA-core kernel and for the tensor-core kernel (3xTF32 split, every k8 step
+accumulated separately and added in FP32)."""
 import ctypes
 
 import pytest
