@@ -213,9 +213,11 @@ struct Engine final : EngineBase {
   int mmax = 40;
   bool use_tc = true;  // tensor-core GEMMs in the mixed path
   // Krylov truncation tolerance of every local exponential (error estimate
-  // beta_j |(exp(-i tau T) e_1)_j|).  Thousands of local steps accumulate it, so the
-  // mixed path keeps it well below its 1e-5 population budget.
-  double lz_tol = std::is_same<T, double>::value ? 1e-12 : 1e-9;
+  // beta_j |(exp(-i tau T) e_1)_j|).  The mixed path's accuracy is set by its FP32
+  // storage (about 1e-7 relative per local update); 1e-7 keeps the Krylov
+  // truncation at that level (tighter values add iterations without changing
+  // the measured population error).
+  double lz_tol = std::is_same<T, double>::value ? 1e-12 : 1e-7;
   // descriptor staging (pinned host + device), bump allocated, reset after a sync
   char* h_stage = nullptr;
   char* d_stage = nullptr;
