@@ -283,7 +283,8 @@ def run_tdvp(args, dist: Dist):
                 "frac": round(tflops / pk["bf16_tflops"], 5), "traffic": None,
                 "peak_source": f"{pk['source']} bf16 dense", "measured_kernel": "gemm",
                 "kernel_time_share": {k: round(v["ms"] / max(1e-9, sum(x["ms"] for x in ks.values())), 4)
-                                      for k, v in ks.items()}}
+                                      for k, v in ks.items()},
+                "kernel_ms_per_step": round(sum(x["ms"] for x in ks.values()) / args.steps, 3)}
     # end to end through the public API with host buffers: upload the warmed-up
     # states (pinned host -> device), evolve, read the populations every step
     e2e = None

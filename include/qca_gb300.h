@@ -130,7 +130,9 @@ int qca_engine_create(int precision, size_t hbm_budget_bytes, qca_engine** out);
 int qca_engine_destroy(qca_engine* e);
 /* Device bytes a chain of this description would hold (admission estimate). */
 int qca_chain_footprint(const qca_chain_desc* d, int precision, size_t* bytes);
-/* TDVP.__init__ (tdvp.py:12-40): upload, canonicalise, build right environments.
+/* TDVP.__init__ (tdvp.py:12-40): upload now; canonicalisation and the right
+ * environments run at the next step/measure/get_mps call, grouped over every chain
+ * added before it (one launch per sweep position for all of them).
  * Returns QCA_ERR_ADMISSION when the budget would be exceeded. */
 int qca_chain_add(qca_engine* e, const qca_chain_desc* d, void* stream, int* chain_id);
 int qca_chain_remove(qca_engine* e, int chain_id);

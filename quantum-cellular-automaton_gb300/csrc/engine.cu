@@ -157,6 +157,7 @@ struct Chain {
   int lz_used = 0;    // largest Krylov dimension in the current step
   double disc_host = 0.0;
   int status = 0;
+  bool pending_init = false;  // uploaded, TDVP.__init__ not yet run
   cplx<T>* cur(int i) { return A[par[i]][i]; }
   cplx<T>* alt(int i) { return A[par[i] ^ 1][i]; }
 };
@@ -933,32 +934,63 @@ struct Engine final : EngineBase {
   // orthonormal tensors left out (LAPACK's QR returns R = I for them):
   //   left sweep to N-1, right sweep to 0, left sweep to N-2,
   //   R env at N-1, then for site N-2..1: right QR at site, R env at site.
-  int init_chain(Chain<T>* c, cudaStream_t st) {
-    const int N = c->N;
-    for (int s = 0; s < N - 1; ++s) {
-      std::vector<MoveJob> J{MoveJob{c, s, true}};
+  // Run for every chain added since the last operation, in lock step: sweep
+  // position t of every chain shares one grouped launch (right sweeps aligned at
+  // each chain's last site).  Each chain sees the same operations in the same
+  // order as when initialised alone.
+  int init_many(std::vector<Chain<T>*>& C, cudaStream_t st) {
+    int maxN = 0;
+    for (auto* c : C) maxN = std::max(maxN, c->N);
+    for (int s = 0; s + 1 < maxN; ++s) {
+      std::vector<MoveJob> J;
+      for (auto* c : C)
+        if (s < c->N - 1) J.push_back(MoveJob{c, s, true});
       QCA_TRY(qr_moves(J, st));
     }
-    for (int s = N - 1; s >= 1; --s) {
-      std::vector<MoveJob> J{MoveJob{c, s, false}};
+    for (int t = 0; t + 1 < maxN; ++t) {  // site N-1-t
+      std::vector<MoveJob> J;
+      for (auto* c : C)
+        if (c->N - 1 - t >= 1) J.push_back(MoveJob{c, c->N - 1 - t, false});
       QCA_TRY(qr_moves(J, st));
     }
-    for (int s = 0; s < N - 2; ++s) {
-      std::vector<MoveJob> J{MoveJob{c, s, true}};
+    for (int s = 0; s + 2 < maxN; ++s) {
+      std::vector<MoveJob> J;
+      for (auto* c : C)
+        if (s < c->N - 2) J.push_back(MoveJob{c, s, true});
       QCA_TRY(qr_moves(J, st));
     }
     {
-      std::vector<EnvJob> J{EnvJob{c, N - 1, false}};
+      std::vector<EnvJob> J;
+      for (auto* c : C) J.push_back(EnvJob{c, c->N - 1, false});
       QCA_TRY(env_update(J, st));
     }
-    for (int s = N - 2; s >= 1; --s) {
-      std::vector<MoveJob> J{MoveJob{c, s, false}};
+    for (int t = 0; t + 2 < maxN; ++t) {  // site N-2-t
+      std::vector<MoveJob> J;
+      std::vector<EnvJob> E;
+      for (auto* c : C) {
+        const int s = c->N - 2 - t;
+        if (s < 1) continue;
+        J.push_back(MoveJob{c, s, false});
+        E.push_back(EnvJob{c, s, false});
+      }
       QCA_TRY(qr_moves(J, st));
-      std::vector<EnvJob> E{EnvJob{c, s, false}};
       QCA_TRY(env_update(E, st));
     }
-    c->center = 0;
+    for (auto* c : C) {
+      c->center = 0;
+      c->pending_init = false;
+    }
     return QCA_OK;
+  }
+
+  // initialise every chain still waiting for it (all of them, so that chains
+  // added one at a time share the grouped launches)
+  int ensure_init(cudaStream_t st) {
+    std::vector<Chain<T>*> C;
+    for (auto& kv : chains)
+      if (kv.second->pending_init) C.push_back(kv.second.get());
+    if (C.empty()) return QCA_OK;
+    return init_many(C, st);
   }
 
   // ------------------------------------------------------------------ one tick
@@ -1302,6 +1334,7 @@ struct Engine final : EngineBase {
       for (auto& kv : chains) C.push_back(kv.second.get());
     }
     if (C.empty() || nsteps <= 0) return QCA_OK;
+    QCA_TRY(ensure_init(st));
     // chains whose gauge was moved by a measurement: make_site_canonical(0) and
     // rebuild the right environments (the gauge-consistent start of tdvp.py:54)
     std::vector<Chain<T>*> dirty;
@@ -1341,6 +1374,7 @@ struct Engine final : EngineBase {
       }
       C.push_back(it->second.get());
     }
+    QCA_TRY(ensure_init(st));
     size_t ob = 0;
     for (auto* c : C) {
       if (bonds_out)
@@ -1357,6 +1391,7 @@ struct Engine final : EngineBase {
     for (size_t i = 0; i < C.size(); ++i) keep[i] = C[i]->algo == QCA_ALGO_2TDVP && C[i]->center == 0;
     std::vector<const cplx<T>*> cen(C.size(), nullptr);
     for (size_t i = 0; i < C.size(); ++i) cen[i] = C[i]->cur(0);
+    const std::vector<Span> sp = spans();
     for (int k = maxN - 1; k >= 1; --k) {
       std::vector<MoveJob> J;
       for (size_t i = 0; i < C.size(); ++i)
@@ -1422,11 +1457,18 @@ struct Engine final : EngineBase {
           for (size_t k = 0; k < who.size(); ++k) cen[who[k]] = g[k].C;
         }
       }
+      std::vector<RhoDesc<T>> rd;
       for (size_t i = 0; i < C.size(); ++i) {
         Chain<T>* c = C[i];
         if (s >= c->N) continue;
         const cplx<T>* a = keep[i] ? cen[i] : c->cur(s);
-        QCA_TRY(timed(KC_MISC, 0, 0, st, [&] { return launch_rho<T>(a, c->D[s], c->D[s + 1], c->dscal + 8 + 4 * s, st); }));
+        if (!in_spans<T>(sp, a, 2LL * c->D[s] * c->D[s + 1] - 1)) return bad("rho");
+        rd.push_back(RhoDesc<T>{a, c->D[s], c->D[s + 1], c->dscal + 8 + 4 * s});
+      }
+      if (!rd.empty()) {
+        const RhoDesc<T>* dr;
+        QCA_TRY(upload(rd, st, &dr));
+        QCA_TRY(timed(KC_MISC, 0, 0, st, [&] { return launch_rho<T>(dr, (int)rd.size(), st); }));
       }
     }
     std::vector<std::vector<double>> rho(C.size());
@@ -1481,6 +1523,7 @@ struct Engine final : EngineBase {
       return QCA_ERR_INVALID;
     }
     Chain<T>* c = it->second.get();
+    QCA_TRY(ensure_init(st));
     size_t need = 0;
     for (int i = 0; i < c->N; ++i) need += 4ull * c->D[i] * c->D[i + 1];
     if (capd < need) {
@@ -1709,33 +1752,37 @@ int Engine<T>::add(const qca_chain_desc* d, cudaStream_t st, int* id_out) {
   c->sv = (double*)(base + offs[k++]);
   c->dscal = (double*)(base + offs[k++]);
   c->iflags = (int*)(base + offs[k++]);
-  // entry lists
+  // entry lists: laid out back to back at the end of the allocation, uploaded as
+  // one host image
   std::vector<EL> els;
+  const size_t lbase = loffs.empty() ? Lo.total : loffs[0];
+  std::vector<char> limg(Lo.total - lbase, 0);
   for (size_t li = 0; li < lists.size(); ++li) {
     EL e;
     e.ent = (const WEntry*)(base + loffs[2 * li]);
     e.begin = (const int*)(base + loffs[2 * li + 1]);
     e.nout = lists[li].nout;
     if (!lists[li].ent.empty())
-      QCA_CUDA(cudaMemcpyAsync((void*)e.ent, lists[li].ent.data(), sizeof(WEntry) * lists[li].ent.size(),
-                               cudaMemcpyHostToDevice, st));
-    QCA_CUDA(cudaMemcpyAsync((void*)e.begin, lists[li].begin.data(), sizeof(int) * (lists[li].nout + 1),
-                             cudaMemcpyHostToDevice, st));
+      memcpy(limg.data() + (loffs[2 * li] - lbase), lists[li].ent.data(), sizeof(WEntry) * lists[li].ent.size());
+    memcpy(limg.data() + (loffs[2 * li + 1] - lbase), lists[li].begin.data(), sizeof(int) * (lists[li].nout + 1));
     els.push_back(e);
   }
+  if (!limg.empty())
+    QCA_CUDA(cudaMemcpyAsync(base + lbase, limg.data(), limg.size(), cudaMemcpyHostToDevice, st));
   size_t li = 0;
   for (int i = 0; i < N; ++i) c->mv1.push_back(els[li++]);
   for (int i = 0; i + 1 < N; ++i) c->mv2.push_back(els[li++]);
   for (int i = 0; i < N; ++i) c->envl.push_back(els[li++]);
   for (int i = 0; i < N; ++i) c->envr.push_back(els[li++]);
   // upload the MPS and the boundary environments
+  size_t total = 0;
+  for (int i = 0; i < N; ++i) total += 2ull * c->D[i] * c->D[i + 1];
+  std::vector<cplx<T>> tmp(total);
+  for (size_t e = 0; e < total; ++e) tmp[e] = mk<T>((T)d->mps[2 * e], (T)d->mps[2 * e + 1]);
   size_t aoff = 0;
   for (int i = 0; i < N; ++i) {
     const size_t cnt = 2ull * c->D[i] * c->D[i + 1];
-    std::vector<cplx<T>> tmp(cnt);
-    for (size_t e = 0; e < cnt; ++e) tmp[e] = mk<T>((T)d->mps[2 * (aoff + e)], (T)d->mps[2 * (aoff + e) + 1]);
-    QCA_CUDA(cudaMemcpyAsync(c->A[0][i], tmp.data(), sizeof(cplx<T>) * cnt, cudaMemcpyHostToDevice, st));
-    QCA_CUDA(cudaStreamSynchronize(st));
+    QCA_CUDA(cudaMemcpyAsync(c->A[0][i], tmp.data() + aoff, sizeof(cplx<T>) * cnt, cudaMemcpyHostToDevice, st));
     aoff += cnt;
   }
   const cplx<T> one = mk<T>(1, 0);
@@ -1748,12 +1795,9 @@ int Engine<T>::add(const qca_chain_desc* d, cudaStream_t st, int* id_out) {
   raw->id = next_id++;
   chains[raw->id] = std::move(c);
   used += raw->bytes;
-  int s = init_chain(raw, st);
-  if (s == QCA_OK) s = sync(st);
-  if (s != QCA_OK) {
-    remove(raw->id);
-    return s;
-  }
+  // TDVP.__init__ runs at the next operation, grouped with every chain added
+  // before it
+  raw->pending_init = true;
   *id_out = raw->id;
   return QCA_OK;
 }

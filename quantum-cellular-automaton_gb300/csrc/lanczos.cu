@@ -424,9 +424,12 @@ __global__ void copy_kernel(const CopyDesc<T>* __restrict__ descs, int nd) {
 }
 
 template <typename T>
-__global__ void rho_kernel(const cplx<T>* A, int Dl, int Dr, double* out) {
+__global__ void rho_kernel(const RhoDesc<T>* __restrict__ descs) {
   __shared__ double red[33];
-  const long long blk = (long long)Dl * Dr;
+  const RhoDesc<T>& D = descs[blockIdx.x];
+  const cplx<T>* A = D.A;
+  double* out = D.out;
+  const long long blk = (long long)D.Dl * D.Dr;
   double r00 = 0, r11 = 0, r01r = 0, r01i = 0;
   for (long long e = threadIdx.x; e < blk; e += blockDim.x) {
     const cplx<T> a = A[e], b = A[blk + e];
@@ -515,8 +518,9 @@ int launch_copy(const CopyDesc<T>* d, const CopyDesc<T>* h, int nd, cudaStream_t
 }
 
 template <typename T>
-int launch_rho(const cplx<T>* A, int Dl, int Dr, double* rho_out, cudaStream_t st) {
-  rho_kernel<T><<<1, 256, 0, st>>>(A, Dl, Dr, rho_out);
+int launch_rho(const RhoDesc<T>* d, int nd, cudaStream_t st) {
+  if (nd <= 0) return QCA_OK;
+  rho_kernel<T><<<nd, 256, 0, st>>>(d);
   QCA_LAUNCH_CHECK();
   return QCA_OK;
 }
@@ -529,7 +533,7 @@ int launch_rho(const cplx<T>* A, int Dl, int Dr, double* rho_out, cudaStream_t s
   template int launch_lz_normalize<T>(const LanczosDesc<T>*, const LanczosDesc<T>*, int, int, cudaStream_t);      \
   template int launch_lz_combine<T>(const LanczosDesc<T>*, const LanczosDesc<T>*, int, cudaStream_t);             \
   template int launch_copy<T>(const CopyDesc<T>*, const CopyDesc<T>*, int, cudaStream_t);                         \
-  template int launch_rho<T>(const cplx<T>*, int, int, double*, cudaStream_t);
+  template int launch_rho<T>(const RhoDesc<T>*, int, cudaStream_t);
 
 QCA_INST(double)
 QCA_INST(float)

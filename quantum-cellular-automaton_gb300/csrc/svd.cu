@@ -4,19 +4,29 @@
 // and s renormalised (lautils.normalize, lautils.py:4-5).
 //
 // One-sided (Hestenes) Jacobi on the narrower orientation W (mx >= nx):
-// W = Theta when 2 Dr <= 2 Dl, else W = Theta^H.  Its columns are distributed
-// over the shared memory of a thread-block cluster (1..16 CTAs, distributed
-// shared memory); in every round of a round-robin tournament each warp rotates
-// one disjoint column pair, reading and writing both columns through DSMEM, and
-// the cluster barrier separates the rounds.  The same rotations accumulate V
-// (nx x nx), kept beside X in distributed shared memory when the cluster has
-// room and in global memory otherwise.  At convergence X = W V has orthogonal
-// columns whose FP64 norms are the singular values; the site tensors are written
-// directly from X and V:
+// W = Theta when 2 Dr <= 2 Dl, else W = Theta^H, with the rotations accumulated
+// into V (nx x nx).  At convergence X = W V has orthogonal columns whose FP64
+// norms are the singular values; the site tensors are written directly from X
+// and V:
 //   W = Theta:    U = X / sigma,  Vh = V^H
 //   W = Theta^H:  U = V,          Vh = (X / sigma)^H
 // with the renormalised singular values multiplied into A_r (right sweep) or
 // A_l (left sweep), tdvp.py:121-122 and 141-142.
+//
+// Two kernels over a thread-block cluster (1..16 CTAs, distributed shared memory):
+//  * svd_block_kernel (column length <= 256): the columns form 2P blocks of at most
+//    16; CTA k holds two of them in its own shared memory and rotates every pair
+//    between and (once per sweep) inside them with block-local barriers, one column
+//    pair per warp.  After each block round the blocks move one position along the
+//    Brent-Luk ring (position 0 fixed), so 2P - 1 block rounds meet every block pair
+//    once per sweep; only these moves use distributed shared memory and the cluster
+//    barrier.
+//  * svd_cluster_kernel (longer columns): the columns stay where they were loaded,
+//    every round of a round-robin tournament rotates one disjoint column pair per
+//    warp through distributed shared memory, and the cluster barrier separates the
+//    rounds.
+// Column norms are evaluated at the start of every sweep (block round) and updated
+// in closed form by each rotation (a' = a - t|g|, b' = b + t|g|).
 #include <cooperative_groups.h>
 
 #include "tdvp_kernels.cuh"
@@ -30,6 +40,8 @@ namespace {
 constexpr int kSvdThreads = 512;
 constexpr int kSvdMaxN = 1024;
 constexpr int kSvdMaxSweeps = 24;
+constexpr int kSvdBlk = 16;              // columns per block of svd_block_kernel
+constexpr size_t kSvdSmem = 200 * 1024;  // dynamic shared memory per CTA
 
 template <typename T>
 struct Prec;
@@ -75,18 +87,20 @@ struct DF {
   __device__ __forceinline__ float value() const { return hi + lo; }
 };
 
+// Warp-wide sums over the RPL elements each lane holds.  In FP32 the sums are
+// compensated (each product split exactly with an FMA, partial sums carried as
+// hi + lo pairs, also through the warp reduction), so that small inner products of
+// nearly orthogonal columns are resolved beyond the sqrt(m) eps32 noise of a plain
+// FP32 sum and the rotations can drive the columns to FP32-level orthogonality.
+// Every lane returns lane 0's result, so that all lanes of a warp take the same
+// branch and apply the same rotation.
 template <typename T, int RPL>
-__device__ __forceinline__ void pair_gram(const cplx<T> (&ru)[RPL], const cplx<T> (&rv)[RPL], T& al, T& be, T& gr,
-                                          T& gi) {
+__device__ __forceinline__ void pair_cross(const cplx<T> (&ru)[RPL], const cplx<T> (&rv)[RPL], T& gr, T& gi) {
   if constexpr (sizeof(T) == 4) {
-    DF a, b, r, i;
+    DF r, i;
 #pragma unroll
     for (int k = 0; k < RPL; ++k) {
       const cplx<T> u = ru[k], v = rv[k];
-      a.add_prod(u.re, u.re);
-      a.add_prod(u.im, u.im);
-      b.add_prod(v.re, v.re);
-      b.add_prod(v.im, v.im);
       r.add_prod(u.re, v.re);  // conj(u) v
       r.add_prod(u.im, v.im);
       i.add_prod(u.re, v.im);
@@ -94,187 +108,149 @@ __device__ __forceinline__ void pair_gram(const cplx<T> (&ru)[RPL], const cplx<T
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      a.add_df(__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o));
-      b.add_df(__shfl_xor_sync(0xffffffffu, b.hi, o), __shfl_xor_sync(0xffffffffu, b.lo, o));
       r.add_df(__shfl_xor_sync(0xffffffffu, r.hi, o), __shfl_xor_sync(0xffffffffu, r.lo, o));
       i.add_df(__shfl_xor_sync(0xffffffffu, i.hi, o), __shfl_xor_sync(0xffffffffu, i.lo, o));
     }
-    al = a.value();
-    be = b.value();
     gr = r.value();
     gi = i.value();
   } else {
-    T a = 0, b = 0, r = 0, i = 0;
+    T r = 0, i = 0;
 #pragma unroll
     for (int k = 0; k < RPL; ++k) {
       const cplx<T> u = ru[k], v = rv[k];
-      a = fma(u.re, u.re, fma(u.im, u.im, a));
-      b = fma(v.re, v.re, fma(v.im, v.im, b));
       r = fma(u.re, v.re, fma(u.im, v.im, r));
       i = fma(u.re, v.im, fma(-u.im, v.re, i));
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      a += __shfl_xor_sync(0xffffffffu, a, o);
-      b += __shfl_xor_sync(0xffffffffu, b, o);
       r += __shfl_xor_sync(0xffffffffu, r, o);
       i += __shfl_xor_sync(0xffffffffu, i, o);
     }
-    al = a;
-    be = b;
     gr = r;
     gi = i;
+  }
+  gr = __shfl_sync(0xffffffffu, gr, 0);
+  gi = __shfl_sync(0xffffffffu, gi, 0);
+}
+
+template <typename T, int RPL>
+__device__ __forceinline__ T col_norm2(const cplx<T> (&ru)[RPL]) {
+  T a;
+  if constexpr (sizeof(T) == 4) {
+    DF d;
+#pragma unroll
+    for (int k = 0; k < RPL; ++k) {
+      d.add_prod(ru[k].re, ru[k].re);
+      d.add_prod(ru[k].im, ru[k].im);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) d.add_df(__shfl_xor_sync(0xffffffffu, d.hi, o), __shfl_xor_sync(0xffffffffu, d.lo, o));
+    a = d.value();
+  } else {
+    a = 0;
+#pragma unroll
+    for (int k = 0; k < RPL; ++k) a = fma(ru[k].re, ru[k].re, fma(ru[k].im, ru[k].im, a));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+  }
+  return __shfl_sync(0xffffffffu, a, 0);
+}
+
+template <typename T, int RPL>
+__device__ __forceinline__ void col_load(const cplx<T>* p, int len, cplx<T> (&r)[RPL]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 0; k < RPL; ++k) {
+    const int i = lane + 32 * k;
+    r[k] = i < len ? p[i] : mk<T>(0, 0);
   }
 }
 
 template <typename T, int RPL>
-__global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<T>* __restrict__ descs, int cs,
-                                                                  int cpc, int v_smem) {
-  cg::cluster_group cluster = cg::this_cluster();
-  const int rank = (int)cluster.block_rank();
-  const SvdDesc<T>& D = descs[blockIdx.x / cs];
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  cplx<T>* Xloc = reinterpret_cast<cplx<T>*>(smem_raw);  // cpc columns of mx elements
-  __shared__ double snorm[kSvdMaxN];                     // used in CTA 0
-  __shared__ int perm[kSvdMaxN];                         // used in CTA 0
-  __shared__ int s_flag[2];                              // rotation flags (CTA 0), by sweep parity
-  __shared__ int s_k;
-  __shared__ double s_keep;
-  __shared__ double s_fro;  // ||Theta||_F^2 (CTA 0)
-  __shared__ double red[33];
-  const int Dl = D.Dl, Dr = D.Dr;
-  const int m = 2 * Dl, n = 2 * Dr;
-  const bool trans = n > m;
-  const int mx = trans ? n : m;
-  const int nx = trans ? m : n;
-  const long long blk = (long long)Dl * Dr;
-  // V columns: after X in shared memory, or slot-major in the global workspace
-  cplx<T>* Vloc = v_smem ? Xloc + (long long)cpc * mx : D.work + (long long)rank * cpc * nx;
-  for (int lc = 0; lc < cpc; ++lc) {
-    const int col = rank * cpc + lc;
-    if (col >= nx) break;
-    for (int row = threadIdx.x; row < nx; row += blockDim.x)
-      Vloc[(long long)lc * nx + row] = mk<T>(row == col ? (T)1 : (T)0, (T)0);
+__device__ __forceinline__ void col_store(cplx<T>* p, int len, const cplx<T> (&r)[RPL]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 0; k < RPL; ++k) {
+    const int i = lane + 32 * k;
+    if (i < len) p[i] = r[k];
   }
-  // load my columns of W
-  for (int lc = 0; lc < cpc; ++lc) {
-    const int col = rank * cpc + lc;
-    if (col >= nx) break;
-    for (int row = threadIdx.x; row < mx; row += blockDim.x) {
+}
+
+// One Jacobi rotation of the column pair (xu, xv) of X, applied to (vu, vv) of V,
+// all held in registers; al, be are the squared column norms on entry and exit.
+// Returns false (nothing changed) when the pair is already orthogonal to the
+// tolerance or one column is at the rounding floor of the matrix.
+//   x_p' = c x_p - s e^{-i phi} x_q ;  x_q' = s e^{i phi} x_p + c x_q   (unitary)
+template <typename T, int RPL>
+__device__ __forceinline__ bool jacobi_rotate(cplx<T> (&xu)[RPL], cplx<T> (&xv)[RPL], cplx<T> (&vu)[RPL],
+                                              cplx<T> (&vv)[RPL], T& al, T& be, double tol, T floor2) {
+  T gr, gi;
+  pair_cross<T, RPL>(xu, xv, gr, gi);
+  const T g = sqrt(gr * gr + gi * gi);
+  if (!(g > (T)tol * sqrt(al * be)) || al <= floor2 || be <= floor2) return false;
+  const T zeta = (be - al) / (2 * g);
+  const T t = (zeta >= 0 ? (T)1 : (T)-1) / (fabs(zeta) + sqrt(1 + zeta * zeta));
+  const T c = 1 / sqrt(1 + t * t);
+  const T s = c * t;
+  const T er = gr / g, ei = gi / g;  // e^{i phi}
+  const cplx<T> smq = mk<T>(-s * er, s * ei);
+  const cplx<T> spq = mk<T>(s * er, s * ei);
+#pragma unroll
+  for (int r = 0; r < RPL; ++r) {
+    const cplx<T> a = xu[r], b = xv[r];
+    xu[r] = c * a + smq * b;
+    xv[r] = spq * a + c * b;
+    const cplx<T> va = vu[r], vb = vv[r];
+    vu[r] = c * va + smq * vb;
+    vv[r] = spq * va + c * vb;
+  }
+  T aln = al - t * g, ben = be + t * g;
+  if (aln < (T)0.01 * al || ben < (T)0.01 * be) {
+    // cancellation in the closed-form update: re-evaluate from the rotated columns
+    aln = col_norm2<T, RPL>(xu);
+    ben = col_norm2<T, RPL>(xv);
+  }
+  al = aln;
+  be = ben;
+  return true;
+}
+
+// W column col (mx rows) into dst, by the whole CTA
+template <typename T>
+__device__ __forceinline__ void load_w_column(const SvdDesc<T>& D, bool trans, int mx, int nx, int col, cplx<T>* dst) {
+  const int Dl = D.Dl, Dr = D.Dr;
+  const long long blk = (long long)Dl * Dr;
+  for (int row = threadIdx.x; row < mx; row += blockDim.x) {
+    cplx<T> v = mk<T>(0, 0);
+    if (col < nx) {
       const int r = trans ? col : row;
       const int c = trans ? row : col;
       const int s1 = r / Dl, a = r - s1 * Dl, s2 = c / Dr, cc = c - s2 * Dr;
-      cplx<T> v = D.theta[(long long)(s1 * 2 + s2) * blk + (long long)a * Dr + cc];
+      v = D.theta[(long long)(s1 * 2 + s2) * blk + (long long)a * Dr + cc];
       if (trans) v.im = -v.im;
-      Xloc[(long long)lc * mx + row] = v;
     }
+    dst[row] = v;
   }
-  if (threadIdx.x < 2) s_flag[threadIdx.x] = 0;
-  if (threadIdx.x == 0) s_fro = 0.0;
-  cluster.sync();
-  {
-    // Frobenius norm: columns whose norm is at the rounding floor of the matrix
-    // carry no information; rotating them against large columns only re-injects
-    // rounding noise and would keep the sweeps from terminating.
-    double f = 0.0;
-    for (int lc = 0; lc < cpc; ++lc) {
-      if (rank * cpc + lc >= nx) break;
-      for (int row = threadIdx.x; row < mx; row += blockDim.x) f += (double)norm2(Xloc[(long long)lc * mx + row]);
-    }
-    f = block_sum(f, red);
-    if (threadIdx.x == 0) atomicAdd(cluster.map_shared_rank(&s_fro, 0), f);
-  }
-  cluster.sync();
-  const double fro = *cluster.map_shared_rank(&s_fro, 0);
+}
+
+// After convergence: FP64 norms of the columns (singular values), rank sort in CTA 0,
+// the truncation rule, and the site tensors from the kept columns.  L.own(j) says
+// whether this CTA holds global column j, L.x(j) / L.v(j) give its X (mx) and V (nx)
+// columns.  Ends with a cluster barrier: CTA 0's shared memory is read through
+// distributed shared memory until then.
+template <typename T, typename Loc>
+__device__ void svd_finish(const SvdDesc<T>& D, cg::cluster_group& cluster, int rank, const Loc& L, int mx, int nx,
+                           bool trans, int sweep, T floor2, double* snorm, int* perm, int* s_k, double* s_keep) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const int P = nx + (nx & 1);
-  const double tol = Prec<T>::eps * (sizeof(T) == 4 ? 8.0 : fmax(8.0, 2.0 * sqrt((double)mx)));
-  const T floor2 = (T)(16.0 * Prec<T>::eps * Prec<T>::eps * fro);
-  int* flag0 = cluster.map_shared_rank(s_flag, 0);
-  int sweep = 0;
-  for (; sweep < kSvdMaxSweeps; ++sweep) {
-    const int par = sweep & 1;
-    int rotated = 0;
-    for (int round = 0; round < P - 1; ++round) {
-      for (int pk = rank + cs * wid; pk < P / 2; pk += cs * nw) {
-        int p, q;
-        if (pk == 0) {
-          p = P - 1;
-          q = round;
-        } else {
-          p = (round + pk) % (P - 1);
-          q = (round - pk + P - 1) % (P - 1);
-        }
-        if (p >= nx || q >= nx) continue;
-        if (p > q) {
-          const int t = p;
-          p = q;
-          q = t;
-        }
-        cplx<T>* xp = cluster.map_shared_rank(Xloc, p / cpc) + (long long)(p % cpc) * mx;
-        cplx<T>* xq = cluster.map_shared_rank(Xloc, q / cpc) + (long long)(q % cpc) * mx;
-        cplx<T>* vp = (v_smem ? cluster.map_shared_rank(Xloc, p / cpc) + (long long)cpc * mx
-                              : D.work + (long long)(p / cpc) * cpc * nx) + (long long)(p % cpc) * nx;
-        cplx<T>* vq = (v_smem ? cluster.map_shared_rank(Xloc, q / cpc) + (long long)cpc * mx
-                              : D.work + (long long)(q / cpc) * cpc * nx) + (long long)(q % cpc) * nx;
-        // both columns of X and of V staged in registers in one round of (possibly
-        // remote) loads; the Gram entries and the rotation in the working precision T
-        // (the singular values are re-evaluated in FP64 after convergence)
-        cplx<T> ru[RPL], rv[RPL], wu[RPL], wv[RPL];
-#pragma unroll
-        for (int r = 0; r < RPL; ++r) {
-          const int i = lane + 32 * r;
-          ru[r] = i < mx ? xp[i] : mk<T>(0, 0);
-          rv[r] = i < mx ? xq[i] : mk<T>(0, 0);
-          wu[r] = i < nx ? vp[i] : mk<T>(0, 0);
-          wv[r] = i < nx ? vq[i] : mk<T>(0, 0);
-        }
-        T al, be, gr, gi;
-        pair_gram<T, RPL>(ru, rv, al, be, gr, gi);
-        const T g = sqrt(gr * gr + gi * gi);
-        if (!(g > (T)tol * sqrt(al * be)) || al <= floor2 || be <= floor2) continue;
-        rotated = 1;
-        const T zeta = (be - al) / (2 * g);
-        const T t = (zeta >= 0 ? (T)1 : (T)-1) / (fabs(zeta) + sqrt(1 + zeta * zeta));
-        const T c = 1 / sqrt(1 + t * t);
-        const T s = c * t;
-        const T er = gr / g, ei = gi / g;  // e^{i phi}
-        // x_p' = c x_p - s e^{-i phi} x_q ; x_q' = s e^{i phi} x_p + c x_q  (unitary)
-        const T cc = c;
-        const cplx<T> smq = mk<T>(-s * er, s * ei);
-        const cplx<T> spq = mk<T>(s * er, s * ei);
-#pragma unroll
-        for (int r = 0; r < RPL; ++r) {
-          const int i = lane + 32 * r;
-          if (i < mx) {
-            xp[i] = cc * ru[r] + smq * rv[r];
-            xq[i] = spq * ru[r] + cc * rv[r];
-          }
-          if (i < nx) {
-            vp[i] = cc * wu[r] + smq * wv[r];
-            vq[i] = spq * wu[r] + cc * wv[r];
-          }
-        }
-      }
-      cluster.sync();
-    }
-    if (rotated && lane == 0) atomicOr(flag0 + par, 1);
-    cluster.sync();
-    const int any = *(volatile int*)(flag0 + par);
-    cluster.sync();  // everyone has read the flag before it is reset below
-    if (rank == 0 && threadIdx.x == 0) s_flag[par] = 0;
-    if (!any) break;
-  }
-  // column norms (FP64) gathered in CTA 0
+  const int Dr = D.Dr;
   double* snorm0 = cluster.map_shared_rank(snorm, 0);
-  for (int lc = wid; lc < cpc; lc += nw) {
-    const int col = rank * cpc + lc;
-    if (col >= nx) break;
-    const cplx<T>* x = Xloc + (long long)lc * mx;
+  for (int j = wid; j < nx; j += nw) {
+    if (!L.own(j)) continue;
+    const cplx<T>* x = L.x(j);
     double s = 0.0;
     for (int i = lane; i < mx; i += 32) s += (double)x[i].re * x[i].re + (double)x[i].im * x[i].im;
     s = warp_sum(s);
-    if (lane == 0) snorm0[col] = sqrt(s);
+    if (lane == 0) snorm0[j] = sqrt(s);
   }
   cluster.sync();
   if (rank == 0) {
@@ -310,8 +286,8 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
       if (k < 1) k = 1;
       double keep = 0.0;
       for (int i = 0; i < k; ++i) keep += snorm[perm[i]] * snorm[perm[i]];
-      s_k = k;
-      s_keep = sqrt(keep);
+      *s_k = k;
+      *s_keep = sqrt(keep);
       *D.k_out = k;
       if (D.discarded) *D.discarded += total > 0 ? (total - keep) / total : 0.0;
       for (int i = 0; i < nx; ++i) D.sv[i] = snorm[perm[i]];
@@ -322,16 +298,15 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
     }
   }
   cluster.sync();
-  const int k = *cluster.map_shared_rank(&s_k, 0);
-  const double keep = *cluster.map_shared_rank(&s_keep, 0);
+  const int k = *cluster.map_shared_rank(s_k, 0);
+  const double keep = *cluster.map_shared_rank(s_keep, 0);
   const int* perm0 = cluster.map_shared_rank(perm, 0);
   const double* sn0 = cluster.map_shared_rank(snorm, 0);
-  // kept columns that live in this CTA
   for (int i = 0; i < k; ++i) {
     const int j = perm0[i];
-    if (j / cpc != rank) continue;
-    const cplx<T>* x = Xloc + (long long)(j % cpc) * mx;
-    const cplx<T>* v = Vloc + (long long)(j % cpc) * nx;
+    if (!L.own(j)) continue;
+    const cplx<T>* x = L.x(j);
+    const cplx<T>* v = L.v(j);
     const double sig = sn0[j];
     const double inv = sig > 0 ? 1.0 / sig : 0.0;
     const double sn = keep > 0 ? sig / keep : 0.0;  // renormalised singular value
@@ -363,9 +338,370 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
       }
     }
   }
-  // CTA 0's shared memory (perm, norms, k) is read through DSMEM above: no CTA may
-  // exit before every CTA of the cluster is done with it.
   cluster.sync();
+}
+
+// columns rank*cpc .. rank*cpc + cpc - 1 of svd_cluster_kernel
+template <typename T>
+struct SlabLoc {
+  const cplx<T>* X;
+  const cplx<T>* V;
+  int cpc, mx, nx, rank;
+  __device__ bool own(int j) const { return j / cpc == rank; }
+  __device__ const cplx<T>* x(int j) const { return X + (long long)(j % cpc) * mx; }
+  __device__ const cplx<T>* v(int j) const { return V + (long long)(j % cpc) * nx; }
+};
+
+// blocks of svd_block_kernel at their sweep-start positions: block be sits in the
+// top slot of CTA be (be < P) or the bottom slot of CTA 2P - 1 - be
+template <typename T>
+struct BlockLoc {
+  const cplx<T>* X;   // [slot][b][mx]
+  const cplx<T>* V;   // [slot][b][nx], or null: V column j at Vg + j nx
+  const cplx<T>* Vg;
+  int P, b, mx, nx, rank;
+  __device__ int blk(int j) const { return j / b; }
+  __device__ int slot(int j) const { return blk(j) < P ? 0 : 1; }
+  __device__ bool own(int j) const { return (blk(j) < P ? blk(j) : 2 * P - 1 - blk(j)) == rank; }
+  __device__ const cplx<T>* x(int j) const { return X + ((long long)slot(j) * b + j % b) * mx; }
+  __device__ const cplx<T>* v(int j) const {
+    return V ? V + ((long long)slot(j) * b + j % b) * nx : Vg + (long long)j * nx;
+  }
+};
+
+template <typename T, int RPL>
+__global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<T>* __restrict__ descs, int cs,
+                                                                  int cpc, int v_smem) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const SvdDesc<T>& D = descs[blockIdx.x / cs];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx<T>* Xloc = reinterpret_cast<cplx<T>*>(smem_raw);  // cpc columns of mx elements
+  __shared__ double snorm[kSvdMaxN];                     // used in CTA 0
+  __shared__ int perm[kSvdMaxN];                         // used in CTA 0
+  __shared__ int s_flag[2];                              // rotation flags (CTA 0), by sweep parity
+  __shared__ int s_k;
+  __shared__ double s_keep;
+  __shared__ double s_fro;  // ||Theta||_F^2 (CTA 0)
+  __shared__ double red[33];
+  __shared__ T s_cn[kSvdMaxN];  // squared norms of this CTA's columns
+  const int m = 2 * D.Dl, n = 2 * D.Dr;
+  const bool trans = n > m;
+  const int mx = trans ? n : m;
+  const int nx = trans ? m : n;
+  // V columns: after X in shared memory, or slot-major in the global workspace
+  cplx<T>* Vloc = v_smem ? Xloc + (long long)cpc * mx : D.work + (long long)rank * cpc * nx;
+  for (int lc = 0; lc < cpc; ++lc) {
+    const int col = rank * cpc + lc;
+    if (col >= nx) break;
+    for (int row = threadIdx.x; row < nx; row += blockDim.x)
+      Vloc[(long long)lc * nx + row] = mk<T>(row == col ? (T)1 : (T)0, (T)0);
+    load_w_column(D, trans, mx, nx, col, Xloc + (long long)lc * mx);
+  }
+  if (threadIdx.x < 2) s_flag[threadIdx.x] = 0;
+  if (threadIdx.x == 0) s_fro = 0.0;
+  cluster.sync();
+  {
+    // Frobenius norm: columns whose norm is at the rounding floor of the matrix
+    // carry no information; rotating them against large columns only re-injects
+    // rounding noise and would keep the sweeps from terminating.
+    double f = 0.0;
+    for (int lc = 0; lc < cpc; ++lc) {
+      if (rank * cpc + lc >= nx) break;
+      for (int row = threadIdx.x; row < mx; row += blockDim.x) f += (double)norm2(Xloc[(long long)lc * mx + row]);
+    }
+    f = block_sum(f, red);
+    if (threadIdx.x == 0) atomicAdd(cluster.map_shared_rank(&s_fro, 0), f);
+  }
+  cluster.sync();
+  const double fro = *cluster.map_shared_rank(&s_fro, 0);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int P = nx + (nx & 1);
+  const double tol = Prec<T>::eps * (sizeof(T) == 4 ? 8.0 : fmax(8.0, 2.0 * sqrt((double)mx)));
+  const T floor2 = (T)(16.0 * Prec<T>::eps * Prec<T>::eps * fro);
+  int* flag0 = cluster.map_shared_rank(s_flag, 0);
+  int sweep = 0;
+  for (; sweep < kSvdMaxSweeps; ++sweep) {
+    const int par = sweep & 1;
+    int rotated = 0;
+    for (int lc = wid; lc < cpc; lc += nw) {
+      if (rank * cpc + lc >= nx) break;
+      cplx<T> ru[RPL];
+      col_load<T, RPL>(Xloc + (long long)lc * mx, mx, ru);
+      const T a = col_norm2<T, RPL>(ru);
+      if (lane == 0) s_cn[lc] = a;
+    }
+    cluster.sync();
+    for (int round = 0; round < P - 1; ++round) {
+      for (int pk = rank + cs * wid; pk < P / 2; pk += cs * nw) {
+        int p, q;
+        if (pk == 0) {
+          p = P - 1;
+          q = round;
+        } else {
+          p = (round + pk) % (P - 1);
+          q = (round - pk + P - 1) % (P - 1);
+        }
+        if (p >= nx || q >= nx) continue;
+        if (p > q) {
+          const int t = p;
+          p = q;
+          q = t;
+        }
+        cplx<T>* xp = cluster.map_shared_rank(Xloc, p / cpc) + (long long)(p % cpc) * mx;
+        cplx<T>* xq = cluster.map_shared_rank(Xloc, q / cpc) + (long long)(q % cpc) * mx;
+        cplx<T>* vp = (v_smem ? cluster.map_shared_rank(Xloc, p / cpc) + (long long)cpc * mx
+                              : D.work + (long long)(p / cpc) * cpc * nx) + (long long)(p % cpc) * nx;
+        cplx<T>* vq = (v_smem ? cluster.map_shared_rank(Xloc, q / cpc) + (long long)cpc * mx
+                              : D.work + (long long)(q / cpc) * cpc * nx) + (long long)(q % cpc) * nx;
+        T* cnp = cluster.map_shared_rank(s_cn, p / cpc) + (p % cpc);
+        T* cnq = cluster.map_shared_rank(s_cn, q / cpc) + (q % cpc);
+        // both columns of X and of V staged in registers in one round of (possibly
+        // remote) loads; the rotation in the working precision T (the singular values
+        // are re-evaluated in FP64 after convergence)
+        cplx<T> ru[RPL], rv[RPL], wu[RPL], wv[RPL];
+        col_load<T, RPL>(xp, mx, ru);
+        col_load<T, RPL>(xq, mx, rv);
+        col_load<T, RPL>(vp, nx, wu);
+        col_load<T, RPL>(vq, nx, wv);
+        T al = *cnp, be = *cnq;
+        if (!jacobi_rotate<T, RPL>(ru, rv, wu, wv, al, be, tol, floor2)) continue;
+        rotated = 1;
+        col_store<T, RPL>(xp, mx, ru);
+        col_store<T, RPL>(xq, mx, rv);
+        col_store<T, RPL>(vp, nx, wu);
+        col_store<T, RPL>(vq, nx, wv);
+        if (lane == 0) {
+          *cnp = al;
+          *cnq = be;
+        }
+      }
+      cluster.sync();
+    }
+    if (rotated && lane == 0) atomicOr(flag0 + par, 1);
+    cluster.sync();
+    const int any = *(volatile int*)(flag0 + par);
+    cluster.sync();  // everyone has read the flag before it is reset below
+    if (rank == 0 && threadIdx.x == 0) s_flag[par] = 0;
+    if (!any) break;
+  }
+  const SlabLoc<T> L{Xloc, Vloc, cpc, mx, nx, rank};
+  svd_finish<T>(D, cluster, rank, L, mx, nx, trans, sweep, floor2, snorm, perm, &s_k, &s_keep);
+}
+
+template <typename T, int RPL>
+__global__ void __launch_bounds__(kSvdThreads) svd_block_kernel(const SvdDesc<T>* __restrict__ descs, int P,
+                                                                int v_smem) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const SvdDesc<T>& D = descs[blockIdx.x / P];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double snorm[kSvdMaxN];  // used in CTA 0
+  __shared__ int perm[kSvdMaxN];      // used in CTA 0
+  __shared__ int s_flag[2];           // rotation flags (CTA 0), by sweep parity
+  __shared__ int s_k;
+  __shared__ double s_keep;
+  __shared__ double s_fro;  // ||Theta||_F^2 (CTA 0)
+  __shared__ double red[33];
+  __shared__ T s_cn[2][kSvdBlk];  // squared norms of the resident columns
+  const int m = 2 * D.Dl, n = 2 * D.Dr;
+  const bool trans = n > m;
+  const int mx = trans ? n : m;
+  const int nx = trans ? m : n;
+  const int n2 = 2 * P;                // blocks (tournament players)
+  const int b = (nx + n2 - 1) / n2;    // columns per block (<= kSvdBlk)
+  // slots [generation][top/bottom][b columns]: X (mx each), then V (nx each) when it
+  // fits, else V column j stays at D.work + j nx (never moved)
+  cplx<T>* Xs = reinterpret_cast<cplx<T>*>(smem_raw);
+  cplx<T>* Vs = v_smem ? Xs + 4LL * b * mx : nullptr;
+  cplx<T>* Vg = D.work;
+  auto xs = [&](int g, int s, int j) { return Xs + ((long long)(g * 2 + s) * b + j) * mx; };
+  auto vc = [&](int g, int s, int j, int gid) {
+    return v_smem ? Vs + ((long long)(g * 2 + s) * b + j) * nx : Vg + (long long)gid * nx;
+  };
+  // block at ring position pos in block round r (circle method, position 0 fixed)
+  auto player = [&](int pos, int r) { return pos == 0 ? 0 : 1 + (pos - 1 + r) % (n2 - 1); };
+  for (int s = 0; s < 2; ++s) {
+    const int be = s == 0 ? rank : n2 - 1 - rank;
+    for (int j = 0; j < b; ++j) {
+      const int col = be * b + j;
+      load_w_column(D, trans, mx, nx, col, xs(0, s, j));
+      if (col < nx || v_smem) {
+        cplx<T>* v = vc(0, s, j, col);
+        for (int row = threadIdx.x; row < nx; row += blockDim.x)
+          v[row] = mk<T>(row == col ? (T)1 : (T)0, (T)0);
+      }
+    }
+  }
+  if (threadIdx.x < 2) s_flag[threadIdx.x] = 0;
+  if (threadIdx.x == 0) s_fro = 0.0;
+  cluster.sync();
+  {
+    // Frobenius norm (padding columns are zero)
+    double f = 0.0;
+    for (int c = 0; c < 2 * b; ++c) {
+      const cplx<T>* x = xs(0, c / b, c % b);
+      for (int row = threadIdx.x; row < mx; row += blockDim.x) f += (double)norm2(x[row]);
+    }
+    f = block_sum(f, red);
+    if (threadIdx.x == 0) atomicAdd(cluster.map_shared_rank(&s_fro, 0), f);
+  }
+  cluster.sync();
+  const double fro = *cluster.map_shared_rank(&s_fro, 0);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const double tol = Prec<T>::eps * (sizeof(T) == 4 ? 8.0 : fmax(8.0, 2.0 * sqrt((double)mx)));
+  const T floor2 = (T)(16.0 * Prec<T>::eps * Prec<T>::eps * fro);
+  int* flag0 = cluster.map_shared_rank(s_flag, 0);
+  int gen = 0, sweep = 0;
+  for (; sweep < kSvdMaxSweeps; ++sweep) {
+    const int par = sweep & 1;
+    int rotated = 0;
+    for (int r = 0; r < n2 - 1; ++r) {
+      const int bt = player(rank, r), bb = player(n2 - 1 - rank, r);
+      for (int c = wid; c < 2 * b; c += nw) {
+        const int s = c / b, j = c - s * b;
+        cplx<T> ru[RPL];
+        col_load<T, RPL>(xs(gen, s, j), mx, ru);
+        const T a = col_norm2<T, RPL>(ru);
+        if (lane == 0) s_cn[s][j] = a;
+      }
+      __syncthreads();
+      if (r == 0) {
+        // pairs inside each resident block, both blocks at once (round robin over b)
+        const int Bp = b + (b & 1), half = Bp / 2;
+        for (int ir = 0; ir + 1 < Bp; ++ir) {
+          for (int t = wid; t < 2 * half; t += nw) {
+            const int s = t / half, pk = t - s * half;
+            int p, q;
+            if (pk == 0) {
+              p = Bp - 1;
+              q = ir;
+            } else {
+              p = (ir + pk) % (Bp - 1);
+              q = (ir - pk + Bp - 1) % (Bp - 1);
+            }
+            if (p >= b || q >= b) continue;
+            const int bl = s == 0 ? bt : bb;
+            const int gp = bl * b + p, gq = bl * b + q;
+            if (gp >= nx || gq >= nx) continue;
+            cplx<T> xu[RPL], xv[RPL], vu[RPL], vv[RPL];
+            col_load<T, RPL>(xs(gen, s, p), mx, xu);
+            col_load<T, RPL>(xs(gen, s, q), mx, xv);
+            col_load<T, RPL>(vc(gen, s, p, gp), nx, vu);
+            col_load<T, RPL>(vc(gen, s, q, gq), nx, vv);
+            T al = s_cn[s][p], be = s_cn[s][q];
+            if (!jacobi_rotate<T, RPL>(xu, xv, vu, vv, al, be, tol, floor2)) continue;
+            rotated = 1;
+            col_store<T, RPL>(xs(gen, s, p), mx, xu);
+            col_store<T, RPL>(xs(gen, s, q), mx, xv);
+            col_store<T, RPL>(vc(gen, s, p, gp), nx, vu);
+            col_store<T, RPL>(vc(gen, s, q, gq), nx, vv);
+            if (lane == 0) {
+              s_cn[s][p] = al;
+              s_cn[s][q] = be;
+            }
+          }
+          __syncthreads();
+        }
+      }
+      {
+        // pairs across the two blocks: warp w keeps top column w in registers and
+        // meets bottom column (w + i) mod b in inner round i
+        const int ga = bt * b + wid;
+        const bool act = wid < b && ga < nx;
+        cplx<T> xu[RPL], vu[RPL];
+        T al = 0;
+        if (act) {
+          col_load<T, RPL>(xs(gen, 0, wid), mx, xu);
+          col_load<T, RPL>(vc(gen, 0, wid, ga), nx, vu);
+          al = s_cn[0][wid];
+        }
+        bool dirty = false;
+        for (int i = 0; i < b; ++i) {
+          if (act) {
+            const int j = (wid + i) % b;
+            const int gb = bb * b + j;
+            if (gb < nx) {
+              cplx<T> xv[RPL], vv[RPL];
+              col_load<T, RPL>(xs(gen, 1, j), mx, xv);
+              col_load<T, RPL>(vc(gen, 1, j, gb), nx, vv);
+              T be = s_cn[1][j];
+              if (jacobi_rotate<T, RPL>(xu, xv, vu, vv, al, be, tol, floor2)) {
+                rotated = 1;
+                dirty = true;
+                col_store<T, RPL>(xs(gen, 1, j), mx, xv);
+                col_store<T, RPL>(vc(gen, 1, j, gb), nx, vv);
+                if (lane == 0) s_cn[1][j] = be;
+              }
+            }
+          }
+          __syncthreads();
+        }
+        if (dirty) {
+          col_store<T, RPL>(xs(gen, 0, wid), mx, xu);
+          col_store<T, RPL>(vc(gen, 0, wid, ga), nx, vu);
+        }
+      }
+      // move the blocks one position along the ring: position p takes the block of
+      // position p + 1, position 2P - 1 the block of position 1, position 0 keeps its
+      // block.  Reads the other CTAs' current generation, writes the own next one.
+      cluster.sync();
+      if (P > 1) {
+        const int ng = gen ^ 1;
+        const int tr = rank == 0 ? 0 : (rank + 1 < P ? rank + 1 : rank);
+        const int ts = rank == 0 ? 0 : (rank + 1 < P ? 0 : 1);
+        const int br = rank >= 1 ? rank - 1 : 1;
+        const int bs = rank >= 1 ? 1 : 0;
+        for (int s = 0; s < 2; ++s) {
+          const int sr = s == 0 ? tr : br, ss = s == 0 ? ts : bs;
+          const cplx<T>* src = cluster.map_shared_rank(xs(gen, ss, 0), sr);
+          cplx<T>* dst = xs(ng, s, 0);
+          for (int e = threadIdx.x; e < b * mx; e += blockDim.x) dst[e] = src[e];
+          if (v_smem) {
+            const cplx<T>* vsrc = cluster.map_shared_rank(vc(gen, ss, 0, 0), sr);
+            cplx<T>* vdst = vc(ng, s, 0, 0);
+            for (int e = threadIdx.x; e < b * nx; e += blockDim.x) vdst[e] = vsrc[e];
+          }
+        }
+        __syncthreads();
+        gen = ng;
+      }
+    }
+    if (rotated && lane == 0) atomicOr(flag0 + par, 1);
+    cluster.sync();
+    const int any = *(volatile int*)(flag0 + par);
+    cluster.sync();  // everyone has read the flag before it is reset below
+    if (rank == 0 && threadIdx.x == 0) s_flag[par] = 0;
+    if (!any) break;
+  }
+  // after a whole sweep (2P - 1 moves) every block is back at its starting position
+  const BlockLoc<T> L{xs(gen, 0, 0), v_smem ? vc(gen, 0, 0, 0) : nullptr, Vg, P, b, mx, nx, rank};
+  svd_finish<T>(D, cluster, rank, L, mx, nx, trans, sweep, floor2, snorm, perm, &s_k, &s_keep);
+}
+
+// block kernel geometry: P CTAs (power of two, P * 32 >= nx where possible), blocks of
+// b <= 16 columns, X (and V when it fits) double-buffered in shared memory
+template <typename T>
+bool svd_block_plan(int mx, int nx, int* P_out, int* b_out, size_t* smem, int* v_smem) {
+  if (mx > 256) return false;
+  int P = 1;
+  while (P * 32 < nx && P < 16) P *= 2;
+  const int b = (nx + 2 * P - 1) / (2 * P);
+  if (b > kSvdBlk) return false;
+  const size_t es = sizeof(cplx<T>);
+  const size_t xb = 4ull * b * mx * es, vb = 4ull * b * nx * es;
+  if (xb + vb <= kSvdSmem) {
+    *v_smem = 1;
+    *smem = xb + vb;
+  } else if (xb <= kSvdSmem) {
+    *v_smem = 0;
+    *smem = xb;
+  } else {
+    return false;
+  }
+  *P_out = P;
+  *b_out = b;
+  return true;
 }
 
 template <typename T>
@@ -395,53 +731,23 @@ int svd_cluster_plan(int mx, int nx, int* cs, int* cpc, size_t* smem, int* v_sme
 // cluster size one problem needs (0 if it does not fit); used to group problems
 template <typename T>
 int svd_cluster_size(int Dl, int Dr) {
-  const int m = 2 * Dl, n = 2 * Dr;
+  const int m = 2 * Dl, n = 2 * Dr, mx = m > n ? m : n, nx = m > n ? n : m;
   int cs, cpc, vs;
   size_t sm;
-  if (svd_cluster_plan<T>(m > n ? m : n, m > n ? n : m, &cs, &cpc, &sm, &vs) != QCA_OK) return 0;
+  if (svd_block_plan<T>(mx, nx, &cs, &cpc, &sm, &vs)) return cs;
+  if (svd_cluster_plan<T>(mx, nx, &cs, &cpc, &sm, &vs) != QCA_OK) return 0;
   return cs;
 }
 
 // shared-memory footprint check used by the host before choosing this path
 template <typename T>
 bool svd_fits(int Dl, int Dr) {
-  const int m = 2 * Dl, n = 2 * Dr;
-  int cs, cpc, vs;
-  size_t sm;
-  return svd_cluster_plan<T>(m > n ? m : n, m > n ? n : m, &cs, &cpc, &sm, &vs) == QCA_OK;
+  return svd_cluster_size<T>(Dl, Dr) > 0;
 }
 
 template <typename T>
-int launch_svd(const SvdDesc<T>* d, const SvdDesc<T>* h, int nd, cudaStream_t st) {
-  if (nd <= 0) return QCA_OK;
-  int mxmax = 1, nxmax = 1;
-  for (int i = 0; i < nd; ++i) {
-    const int m = 2 * h[i].Dl, n = 2 * h[i].Dr;
-    mxmax = std::max(mxmax, std::max(m, n));
-    nxmax = std::max(nxmax, std::min(m, n));
-  }
-  int cs = 1, cpc = 1, vs = 1;
-  size_t smem = 0;
-  if (svd_cluster_plan<T>(mxmax, nxmax, &cs, &cpc, &smem, &vs) != QCA_OK) {
-    set_error("SVD of %d x %d exceeds the distributed shared memory of a 16-CTA cluster", mxmax, nxmax);
-    return QCA_ERR_INVALID;
-  }
-  const int rows = (mxmax + 31) / 32;
-  const int rpl = rows <= 2 ? 2 : rows <= 4 ? 4 : rows <= 8 ? 8 : 16;
-  if (rows > 16) {
-    set_error("SVD column length %d exceeds 512", mxmax);
-    return QCA_ERR_INVALID;
-  }
-  void (*kern)(const SvdDesc<T>*, int, int, int) =
-      rpl == 2 ? svd_cluster_kernel<T, 2>
-               : rpl == 4 ? svd_cluster_kernel<T, 4> : rpl == 8 ? svd_cluster_kernel<T, 8> : svd_cluster_kernel<T, 16>;
-  static bool configured[2][5] = {};
-  const int ti = sizeof(T) == 8 ? 0 : 1, ri = rpl == 2 ? 0 : rpl == 4 ? 1 : rpl == 8 ? 2 : 3;
-  if (!configured[ti][ri]) {
-    QCA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    QCA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    configured[ti][ri] = true;
-  }
+static int launch_cluster(void (*kern)(const SvdDesc<T>*, int, int, int), const SvdDesc<T>* d, int nd, int cs,
+                          int a1, int a2, size_t smem, cudaStream_t st) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(nd * cs, 1, 1);
   cfg.blockDim = dim3(kSvdThreads, 1, 1);
@@ -454,8 +760,73 @@ int launch_svd(const SvdDesc<T>* d, const SvdDesc<T>* h, int nd, cudaStream_t st
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  QCA_CUDA(cudaLaunchKernelEx(&cfg, kern, d, cs, cpc, vs));
+  QCA_CUDA(cudaLaunchKernelEx(&cfg, kern, d, cs, a1, a2));
   return QCA_OK;
+}
+
+template <typename T>
+static int configure(void (*kern)(const SvdDesc<T>*, int, int, int), bool* done) {
+  if (*done) return QCA_OK;
+  QCA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSvdSmem));
+  QCA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  *done = true;
+  return QCA_OK;
+}
+
+template <typename T>
+int launch_svd(const SvdDesc<T>* d, const SvdDesc<T>* h, int nd, cudaStream_t st) {
+  if (nd <= 0) return QCA_OK;
+  int mxmax = 1, nxmax = 1;
+  for (int i = 0; i < nd; ++i) {
+    const int m = 2 * h[i].Dl, n = 2 * h[i].Dr;
+    mxmax = std::max(mxmax, std::max(m, n));
+    nxmax = std::max(nxmax, std::min(m, n));
+  }
+  const int rows = (mxmax + 31) / 32;
+  if (rows > 16) {
+    set_error("SVD column length %d exceeds 512", mxmax);
+    return QCA_ERR_INVALID;
+  }
+  const int rpl = rows <= 2 ? 2 : rows <= 4 ? 4 : rows <= 8 ? 8 : 16;
+  const int ti = sizeof(T) == 8 ? 0 : 1, ri = rpl == 2 ? 0 : rpl == 4 ? 1 : rpl == 8 ? 2 : 3;
+  int P = 1, b = 1, vs = 1;
+  size_t smem = 0;
+  if (svd_block_plan<T>(mxmax, nxmax, &P, &b, &smem, &vs)) {
+    // column length <= 256: RPL <= 8
+    static bool configured[2][3] = {};
+    void (*kern)(const SvdDesc<T>*, int, int) =
+        rpl == 2 ? svd_block_kernel<T, 2> : rpl == 4 ? svd_block_kernel<T, 4> : svd_block_kernel<T, 8>;
+    if (!configured[ti][ri]) {
+      QCA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSvdSmem));
+      QCA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+      configured[ti][ri] = true;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(nd * P, 1, 1);
+    cfg.blockDim = dim3(kSvdThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = P;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    QCA_CUDA(cudaLaunchKernelEx(&cfg, kern, d, P, vs));
+    return QCA_OK;
+  }
+  int cs = 1, cpc = 1;
+  if (svd_cluster_plan<T>(mxmax, nxmax, &cs, &cpc, &smem, &vs) != QCA_OK) {
+    set_error("SVD of %d x %d exceeds the distributed shared memory of a 16-CTA cluster", mxmax, nxmax);
+    return QCA_ERR_INVALID;
+  }
+  static bool configured[2][4] = {};
+  void (*kern)(const SvdDesc<T>*, int, int, int) =
+      rpl == 2 ? svd_cluster_kernel<T, 2>
+               : rpl == 4 ? svd_cluster_kernel<T, 4> : rpl == 8 ? svd_cluster_kernel<T, 8> : svd_cluster_kernel<T, 16>;
+  QCA_TRY(configure<T>(kern, &configured[ti][ri]));
+  return launch_cluster<T>(kern, d, nd, cs, cpc, vs, smem, st);
 }
 
 template int launch_svd<double>(const SvdDesc<double>*, const SvdDesc<double>*, int, cudaStream_t);

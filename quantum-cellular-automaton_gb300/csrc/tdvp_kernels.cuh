@@ -189,8 +189,16 @@ struct CopyDesc {  // dst(i0,i1,i2) = scale * src(i0,i1,i2) with zero padding
 template <typename T>
 int launch_copy(const CopyDesc<T>* d, const CopyDesc<T>* h, int nd, cudaStream_t st);
 
-// single-site reduced density matrices rho[s,s'] = sum_{a,c} A[s][a][c] conj(A[s'][a][c])
+// single-site reduced density matrices rho[s,s'] = sum_{a,c} A[s][a][c] conj(A[s'][a][c]),
+// one CTA per problem; out = {rho00, rho11, Re rho01, Im rho01}
 template <typename T>
-int launch_rho(const cplx<T>* A, int Dl, int Dr, double* rho_out, cudaStream_t st);
+struct RhoDesc {
+  const cplx<T>* A;
+  int Dl, Dr;
+  double* out;
+};
+
+template <typename T>
+int launch_rho(const RhoDesc<T>* d, int nd, cudaStream_t st);
 
 }  // namespace qca
