@@ -170,8 +170,8 @@ int qca_engine_kernel_stats(qca_engine* e, double* out, int reset);
 
 /* Test hook (no counterpart in the reference): C = A B for row-major complex64
  * DEVICE matrices (M x K, K x N, M x N) through the contraction kernels of the
- * mixed path; tensor_cores = 1 selects the 3xTF32 tensor-core kernel, 0 the
- * CUDA-core kernel.  Synchronises the stream. */
+ * mixed path; tensor_cores = 2 selects the 3xTF32 tcgen05 kernel, 1 the 3xTF32
+ * mma.sync kernel, 0 the CUDA-core kernel.  Synchronises the stream. */
 int qca_test_gemm_c64(int M, int N, int K, const void* A, const void* B, void* C, int tensor_cores, void* stream);
 
 #ifdef __cplusplus

@@ -212,7 +212,8 @@ struct Engine final : EngineBase {
   std::map<int, std::unique_ptr<Chain<T>>> chains;
   int next_id = 0;
   int mmax = 40;
-  bool use_tc = true;  // tensor-core GEMMs in the mixed path
+  bool use_tc = true;    // tensor-core GEMMs in the mixed path
+  bool use_umma = true;  // ... with the tcgen05 kernel for M >= kUmmaMinM
   // Krylov truncation tolerance of every local exponential (error estimate
   // beta_j |(exp(-i tau T) e_1)_j|).  The mixed path's accuracy is set by its FP32
   // storage (about 1e-7 relative per local update); 1e-7 keeps the Krylov
@@ -363,30 +364,49 @@ struct Engine final : EngineBase {
       nxx = std::max(nxx, d.N);
     }
     const int cfg = gemm_tile_cfg(mx, nxx);
-    // mixed path: always the 3xTF32 tensor-core kernel, so that a chain's arithmetic
-    // does not depend on which other chains share the launch
-    const bool tc = std::is_same<T, float>::value && use_tc;
-    const int td = tc ? 64 : gemm_tile_dim(cfg);
-    int t = 0;
-    for (auto& d : v) {
-      d.tiles_m = ceil_div(d.M, td);
-      d.tiles_n = ceil_div(d.N, td);
-      d.tile_begin = t;
-      t += d.nb1 * d.nb2 * d.tiles_m * d.tiles_n;
-    }
-    const GemmDesc<T>* dd;
-    QCA_TRY(upload(v, st, &dd));
     double fl = 0.0, by = 0.0;
     for (auto& d : v) {
       const double nb = (double)d.nb1 * d.nb2 * d.G;
       fl += 8.0 * d.M * d.N * (double)d.K * nb;
       by += sizeof(cplx<T>) * ((double)d.M * d.K * nb + (double)d.K * d.N * nb + (double)d.M * d.N * d.nb1 * d.nb2);
     }
+    auto tile = [](std::vector<GemmDesc<T>>& w, int bm, int bn) {
+      int t = 0;
+      for (auto& d : w) {
+        d.tiles_m = ceil_div(d.M, bm);
+        d.tiles_n = ceil_div(d.N, bn);
+        d.tile_begin = t;
+        t += d.nb1 * d.nb2 * d.tiles_m * d.tiles_n;
+      }
+    };
+    if (!std::is_same<T, float>::value || !use_tc) {
+      const int td = gemm_tile_dim(cfg);
+      tile(v, td, td);
+      const GemmDesc<T>* dd;
+      QCA_TRY(upload(v, st, &dd));
+      return timed(KC_GEMM, fl, by, st, [&] { return launch_gemm<T>(dd, v.data(), (int)v.size(), cfg, st); });
+    }
+    // mixed path: 3xTF32 on the tensor cores.  Problems with M >= kUmmaMinM go to the
+    // tcgen05 kernel (128 x 64 tiles), the others to the mma.sync kernel (64 x 64);
+    // the choice depends on the problem's own shape only, so a chain's arithmetic does
+    // not depend on which other chains share the launch.
+    std::vector<GemmDesc<T>> big, small;
+    for (auto& d : v) (use_umma && d.M >= kUmmaMinM ? big : small).push_back(d);
+    tile(big, kUmmaBM, kUmmaBN);
+    tile(small, 64, 64);
+    const GemmDesc<T>* db = nullptr;
+    const GemmDesc<T>* ds = nullptr;
+    if (!big.empty()) QCA_TRY(upload(big, st, &db));
+    if (!small.empty()) QCA_TRY(upload(small, st, &ds));
     return timed(KC_GEMM, fl, by, st, [&] {
-      if (tc)
-        return launch_gemm_tc(reinterpret_cast<const GemmDesc<float>*>(dd),
-                              reinterpret_cast<const GemmDesc<float>*>(v.data()), (int)v.size(), st);
-      return launch_gemm<T>(dd, v.data(), (int)v.size(), cfg, st);
+      int s = QCA_OK;
+      if (!big.empty())
+        s = launch_gemm_umma(reinterpret_cast<const GemmDesc<float>*>(db),
+                             reinterpret_cast<const GemmDesc<float>*>(big.data()), (int)big.size(), st);
+      if (s == QCA_OK && !small.empty())
+        s = launch_gemm_tc(reinterpret_cast<const GemmDesc<float>*>(ds),
+                           reinterpret_cast<const GemmDesc<float>*>(small.data()), (int)small.size(), st);
+      return s;
     });
   }
 
@@ -1356,6 +1376,14 @@ struct Engine final : EngineBase {
       QCA_TRY(tick(act, st));
     }
     QCA_TRY(sync(st));
+    if (std::is_same<T, float>::value && use_tc && use_umma) {
+      int timeouts = 0;
+      QCA_TRY(gemm_umma_timeouts(1, &timeouts));
+      if (timeouts) {
+        set_error("tensor-core GEMM: %d mbarrier waits ran out", timeouts);
+        return QCA_ERR_CUDA;
+      }
+    }
     return QCA_OK;
   }
 

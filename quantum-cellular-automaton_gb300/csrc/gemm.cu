@@ -390,7 +390,8 @@ int launch_gemm_tc(const GemmDesc<float>* d_desc, const GemmDesc<float>* h_desc,
 }  // namespace qca
 
 // Test hook: C = A B for row-major complex64 device matrices through the grouped
-// kernels (tensor_cores: 1 = 3xTF32 tensor-core kernel, 0 = CUDA-core kernel).
+// kernels (tensor_cores: 2 = 3xTF32 tcgen05 kernel, 1 = 3xTF32 mma.sync kernel,
+// 0 = CUDA-core kernel).
 // The single descriptor is passed through a file-scope device slot.
 static __device__ qca::GemmDesc<float> g_test_gemm_slot;
 
@@ -418,9 +419,9 @@ extern "C" int qca_test_gemm_c64(int M, int N, int K, const void* A, const void*
   d.sBn = 1;
   d.sCm = N;
   d.sCn = 1;
-  const int td = 64;
-  d.tiles_m = ceil_div(M, td);
-  d.tiles_n = ceil_div(N, td);
+  const bool um = tensor_cores == 2;
+  d.tiles_m = ceil_div(M, um ? kUmmaBM : 64);
+  d.tiles_n = ceil_div(N, um ? kUmmaBN : 64);
   d.tile_begin = 0;
   GemmDesc<float>* dd = nullptr;
   cudaStream_t st = (cudaStream_t)stream;
@@ -428,8 +429,17 @@ extern "C" int qca_test_gemm_c64(int M, int N, int K, const void* A, const void*
   QCA_CUDA(cudaGetSymbolAddress(&addr, g_test_gemm_slot));
   dd = (GemmDesc<float>*)addr;
   QCA_CUDA(cudaMemcpyAsync(dd, &d, sizeof(d), cudaMemcpyHostToDevice, st));
-  int s = tensor_cores ? launch_gemm_tc(dd, &d, 1, st) : launch_gemm<float>(dd, &d, 1, 2, st);
+  int s = um ? launch_gemm_umma(dd, &d, 1, st)
+             : tensor_cores ? launch_gemm_tc(dd, &d, 1, st) : launch_gemm<float>(dd, &d, 1, 2, st);
   if (s != QCA_OK) return s;
   QCA_CUDA(cudaStreamSynchronize(st));
+  if (um) {
+    int timeouts = 0;
+    QCA_TRY(gemm_umma_timeouts(1, &timeouts));
+    if (timeouts) {
+      set_error("qca_test_gemm_c64: %d tensor-core mbarrier waits ran out", timeouts);
+      return QCA_ERR_CUDA;
+    }
+  }
   return QCA_OK;
 }

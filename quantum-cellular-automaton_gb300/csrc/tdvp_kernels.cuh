@@ -34,6 +34,13 @@ int launch_gemm(const GemmDesc<T>* d_desc, const GemmDesc<T>* h_desc, int ndesc,
 // 3xTF32 tensor-core variant (complex64 operands, 64 x 64 tiles).
 int launch_gemm_tc(const GemmDesc<float>* d_desc, const GemmDesc<float>* h_desc, int ndesc, cudaStream_t st);
 
+// 3xTF32 on the fifth-generation tensor cores (tcgen05.mma, TMEM accumulators),
+// complex64 operands, 128 x 64 tiles; for problems with M >= kUmmaMinM.
+constexpr int kUmmaBM = 128, kUmmaBN = 64, kUmmaMinM = 96;
+int launch_gemm_umma(const GemmDesc<float>* d_desc, const GemmDesc<float>* h_desc, int ndesc, cudaStream_t st);
+// number of tensor-core GEMM mbarrier waits that ran out since the last reset
+int gemm_umma_timeouts(int reset, int* count);
+
 // Tile configuration for a set of problems (0: 16x16, 1: 32x32, 2: 64x64).
 int gemm_tile_cfg(int maxM, int maxN);
 int gemm_tile_dim(int cfg);

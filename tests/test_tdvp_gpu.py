@@ -139,3 +139,36 @@ def test_tdvp_tracks_exact_evolution(alg_name, tol):
         td.measure(*r2)
         worst = max(worst, np.abs(r1[0] - r2[0]).max())
     assert worst < tol, worst
+
+
+@pytest.mark.parametrize("alg_name", ["2tdvp", "1tdvp"])
+def test_tdvp_mixed_tracks_fp64_at_large_bonds(alg_name):
+    """A random MPS with bonds up to 48 (local problems with M = 4 D >= 96 take the
+    tcgen05 contraction kernel): two mixed-precision steps agree with the FP64
+    path (itself pinned to the reference).  The bond cap (96) is above what two
+    steps reach.  Tolerance 3e-5: on this random, highly entangled state the mixed
+    path differs from FP64 by 1.4e-5 (2TDVP) and 1.7e-5 (1TDVP) after two steps,
+    the same with the tcgen05, the mma.sync and the FP32 CUDA-core contraction
+    kernels, i.e. set by the FP32 storage of the state, not by the GEMM."""
+    from qca_gb300 import GpuTDVP, MPO, MPS, Rules
+    n, d, lo, hi, dt, chi = 14, 2, 2, 4, 0.05, 96
+    rng = np.random.default_rng(77)
+    dims = [min(2 ** min(i, n - i), 48) for i in range(n + 1)]
+    A = [(rng.standard_normal((2, dims[i], dims[i + 1])) + 1j * rng.standard_normal((2, dims[i], dims[i + 1])))
+         / np.sqrt(4.0 * dims[i]) for i in range(n)]
+    env = np.ones((1, 1), dtype=np.complex128)
+    for a in A:
+        env = sum(a[s].conj().T @ env @ a[s] for s in range(2))
+    A[0] = A[0] / np.sqrt(env[0, 0].real)
+    H = MPO.hamiltonian_from_rules(Rules(n, range(lo, hi), d))
+    res = []
+    for prec in ("fp64", "mixed"):
+        args = types.SimpleNamespace(step_size=dt, algorithm=alg_name, max_bond_dim=chi, svd_epsilon=1e-10,
+                                     precision=prec)
+        alg = GpuTDVP(MPS.from_tensors(A), H, args)
+        alg.evolve(2)
+        r = rows(n)
+        alg.measure(*r)
+        res.append(r)
+    assert np.abs(res[0][0] - res[1][0]).max() < 3e-5
+
