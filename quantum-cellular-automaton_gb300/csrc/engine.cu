@@ -386,26 +386,48 @@ struct Engine final : EngineBase {
       QCA_TRY(upload(v, st, &dd));
       return timed(KC_GEMM, fl, by, st, [&] { return launch_gemm<T>(dd, v.data(), (int)v.size(), cfg, st); });
     }
-    // mixed path: 3xTF32 on the tensor cores.  Problems with M >= kUmmaMinM go to the
-    // tcgen05 kernel (128 x 64 tiles), the others to the mma.sync kernel (64 x 64);
-    // the choice depends on the problem's own shape only, so a chain's arithmetic does
-    // not depend on which other chains share the launch.
+    // mixed path: 3xTF32 on the tensor cores.  Problems that fill the tcgen05 tile
+    // (M >= kUmmaMinM, N and K >= kUmmaMinNK: 128 x 64 tiles, 16-deep K stages) go to
+    // the tcgen05 kernel, the others to the mma.sync kernel (64 x 64); the choice
+    // depends on the problem's own shape only, so a chain's arithmetic does not depend
+    // on which other chains share the launch.
     std::vector<GemmDesc<T>> big, small;
-    for (auto& d : v) (use_umma && d.M >= kUmmaMinM ? big : small).push_back(d);
+    for (auto& d : v)
+      (use_umma && d.M >= kUmmaMinM && d.N >= kUmmaMinNK && (long long)d.K * d.G >= kUmmaMinNK ? big : small)
+          .push_back(d);
+    // the persistent tcgen05 kernel strides over the tiles: longest K first balances
+    // its CTAs (the order of independent problems changes no arithmetic)
+    std::stable_sort(big.begin(), big.end(), [](const GemmDesc<T>& a, const GemmDesc<T>& b) {
+      return (long long)a.K * a.G > (long long)b.K * b.G;
+    });
     tile(big, kUmmaBM, kUmmaBN);
     tile(small, 64, 64);
     const GemmDesc<T>* db = nullptr;
     const GemmDesc<T>* ds = nullptr;
     if (!big.empty()) QCA_TRY(upload(big, st, &db));
     if (!small.empty()) QCA_TRY(upload(small, st, &ds));
+    const bool both = !big.empty() && !small.empty();
+    if (both) QCA_TRY(ensure_aux());
     return timed(KC_GEMM, fl, by, st, [&] {
       int s = QCA_OK;
-      if (!big.empty())
+      // both kernels at once: the small problems on an auxiliary stream beside the
+      // persistent launch, joined before anything reads their results
+      cudaStream_t s2 = st;
+      if (both) {
+        QCA_CUDA(cudaEventRecord(fork_ev, st));
+        QCA_CUDA(cudaStreamWaitEvent(aux[0], fork_ev, 0));
+        s2 = aux[0];
+      }
+      if (!small.empty())
+        s = launch_gemm_tc(reinterpret_cast<const GemmDesc<float>*>(ds),
+                           reinterpret_cast<const GemmDesc<float>*>(small.data()), (int)small.size(), s2);
+      if (s == QCA_OK && !big.empty())
         s = launch_gemm_umma(reinterpret_cast<const GemmDesc<float>*>(db),
                              reinterpret_cast<const GemmDesc<float>*>(big.data()), (int)big.size(), st);
-      if (s == QCA_OK && !small.empty())
-        s = launch_gemm_tc(reinterpret_cast<const GemmDesc<float>*>(ds),
-                           reinterpret_cast<const GemmDesc<float>*>(small.data()), (int)small.size(), st);
+      if (both) {
+        QCA_CUDA(cudaEventRecord(join_ev[0], aux[0]));
+        QCA_CUDA(cudaStreamWaitEvent(st, join_ev[0], 0));
+      }
       return s;
     });
   }
@@ -492,6 +514,16 @@ struct Engine final : EngineBase {
   cudaStream_t aux[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t fork_ev = nullptr, join_ev[4] = {nullptr, nullptr, nullptr, nullptr};
 
+  int ensure_aux() {
+    if (aux[0]) return QCA_OK;
+    for (int i = 0; i < 4; ++i) {
+      QCA_CUDA(cudaStreamCreateWithFlags(&aux[i], cudaStreamNonBlocking));
+      QCA_CUDA(cudaEventCreateWithFlags(&join_ev[i], cudaEventDisableTiming));
+    }
+    QCA_CUDA(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
+    return QCA_OK;
+  }
+
   int svd_grouped(std::vector<SvdDesc<T>>& sv, cudaStream_t st) {
     std::vector<SvdDesc<T>> grp[5];
     for (auto& d : sv) {
@@ -506,13 +538,7 @@ struct Engine final : EngineBase {
       QCA_TRY(upload(sv, st, &ds));
       return launch_svd<T>(ds, sv.data(), (int)sv.size(), st);
     }
-    if (!aux[0]) {
-      for (int i = 0; i < 4; ++i) {
-        QCA_CUDA(cudaStreamCreateWithFlags(&aux[i], cudaStreamNonBlocking));
-        QCA_CUDA(cudaEventCreateWithFlags(&join_ev[i], cudaEventDisableTiming));
-      }
-      QCA_CUDA(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
-    }
+    QCA_TRY(ensure_aux());
     // descriptors first (stream-ordered copies on st), then fork
     std::vector<const SvdDesc<T>*> dptr(5, nullptr);
     for (int g = 0; g < 5; ++g)

@@ -35,8 +35,9 @@ int launch_gemm(const GemmDesc<T>* d_desc, const GemmDesc<T>* h_desc, int ndesc,
 int launch_gemm_tc(const GemmDesc<float>* d_desc, const GemmDesc<float>* h_desc, int ndesc, cudaStream_t st);
 
 // 3xTF32 on the fifth-generation tensor cores (tcgen05.mma, TMEM accumulators),
-// complex64 operands, 128 x 64 tiles; for problems with M >= kUmmaMinM.
-constexpr int kUmmaBM = 128, kUmmaBN = 64, kUmmaMinM = 96;
+// complex64 operands, 128 x 64 tiles; for problems with M >= kUmmaMinM and N, K >=
+// kUmmaMinNK (smaller problems leave most of the 128 x 64 tile or the pipeline empty).
+constexpr int kUmmaBM = 128, kUmmaBN = 64, kUmmaMinM = 96, kUmmaMinNK = 64;
 int launch_gemm_umma(const GemmDesc<float>* d_desc, const GemmDesc<float>* h_desc, int ndesc, cudaStream_t st);
 // number of tensor-core GEMM mbarrier waits that ran out since the last reset
 int gemm_umma_timeouts(int reset, int* count);
