@@ -331,17 +331,24 @@ def run_e2e(args, specs, states, prec, dist: Dist):
         _lib.call("qca_chain_add", eng.h, ctypes.byref(d), None, ctypes.byref(cid))
         ids.append(cid.value)
     cids = (ctypes.c_int * len(ids))(*ids)
+    t_add = time.perf_counter() - t0
+    t_step = t_meas = 0.0
     for _ in range(args.steps):
-        _lib.call("qca_engine_step_chains", eng.h, cids, len(ids), 1, None)
+        ta = time.perf_counter()
+        _lib.call("qca_engine_step_chains", eng.h, cids, len(ids), 1, None)  # the first also initialises
+        tb = time.perf_counter()
         _lib.call("qca_engine_measure", eng.h, cids, len(ids), pop.ctypes.data_as(_lib._PD),
                   dpop.ctypes.data_as(_lib._PD), sse.ctypes.data_as(_lib._PD), bd.ctypes.data_as(_lib._PD), None)
+        t_step += tb - ta
+        t_meas += time.perf_counter() - tb
     torch.cuda.synchronize()
     el = dist.max(time.perf_counter() - t0)
     su = dist.sum(sum(s.site_updates_per_step() for s in specs) * args.steps)
     del eng
     return {"value": round(su / el, 2), "unit": "site-updates/s", "h2d_bytes_per_step": int(h2d / args.steps),
             "d2h_bytes_per_step": int(d2h), "includes": "chain upload + TDVP init, every step: step + measure "
-            "(populations, entropies, bond dims to host)"}
+            "(populations, entropies, bond dims to host)",
+            "phases_s": {"upload": round(t_add, 3), "init_and_steps": round(t_step, 3), "measure": round(t_meas, 3)}}
 
 
 # ---------------------------------------------------------------- exact workload

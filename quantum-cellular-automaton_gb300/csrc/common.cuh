@@ -94,6 +94,11 @@ __host__ __device__ __forceinline__ void cfma_conj(cplx<T>& acc, cplx<T> a, cplx
 // ----------------------------------------------------------------------------------
 // warp / block reductions in double precision
 // ----------------------------------------------------------------------------------
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

@@ -935,7 +935,7 @@ struct Engine final : EngineBase {
     QCA_TRY(check_qr(q));
     const QrDesc<T>* dq;
     QCA_TRY(upload(q, st, &dq));
-    QCA_TRY(timed(KC_QR, 0, 0, st, [&] { return launch_qr<T>(dq, (int)q.size(), st); }));
+    QCA_TRY(timed(KC_QR, 0, 0, st, [&] { return launch_qr<T>(dq, (int)q.size(), 1, st); }));
     QCA_TRY(run_gemm(g, st));
     for (auto& jb : J) {
       Chain<T>* c = jb.c;
@@ -1177,7 +1177,7 @@ struct Engine final : EngineBase {
       QCA_TRY(check_qr(qr));
       const QrDesc<T>* dq;
       QCA_TRY(upload(qr, st, &dq));
-      QCA_TRY(timed(KC_QR, 0, 0, st, [&] { return launch_qr<T>(dq, (int)qr.size(), st); }));
+      QCA_TRY(timed(KC_QR, 0, 0, st, [&] { return launch_qr<T>(dq, (int)qr.size(), 0, st); }));
     }
     if (!svc.empty()) {
       for (size_t i = 0; i < svc.size(); ++i)
@@ -1506,7 +1506,7 @@ struct Engine final : EngineBase {
           QCA_TRY(check_qr(q));
           const QrDesc<T>* dq;
           QCA_TRY(upload(q, st, &dq));
-          QCA_TRY(timed(KC_QR, 0, 0, st, [&] { return launch_qr<T>(dq, (int)q.size(), st); }));
+          QCA_TRY(timed(KC_QR, 0, 0, st, [&] { return launch_qr<T>(dq, (int)q.size(), 1, st); }));
           QCA_TRY(run_gemm(g, st));
           for (size_t k = 0; k < who.size(); ++k) cen[who[k]] = g[k].C;
         }

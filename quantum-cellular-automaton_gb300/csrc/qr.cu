@@ -10,8 +10,11 @@
 //        v = [1, x / (alpha - beta)],  A[k,k] = beta
 // and H^H = I - conj(tau) v v^H is applied to the trailing columns (zgeqr2).
 // Q = H_0 H_1 ... H_{K-1} is formed explicitly by backward accumulation
-// (zung2r), m x m for the complete factorisation.  One CTA per problem; sums in
-// FP64.
+// (zung2r), m x m for the complete factorisation.  One CTA per problem.  Sums in
+// FP64, except for the mixed path's gauge moves (Acc = float): there the
+// reflector is scaled by the reciprocal of alpha - beta (as zlarfg does) and the
+// dot products of the reflector applications accumulate in FP32, the precision of
+// the stored tensors (FP64 runs at 1/64 of the FP32 rate on this GPU).
 #include "tdvp_kernels.cuh"
 
 namespace qca {
@@ -27,7 +30,7 @@ __device__ __forceinline__ cplx<T> cdiv(cplx<double> a, cplx<double> b) {
   return mk<T>((T)((a.re * b.re + a.im * b.im) / d), (T)((a.im * b.re - a.re * b.im) / d));
 }
 
-template <typename T>
+template <typename T, typename Acc>
 __global__ void __launch_bounds__(kQrThreads) qr_kernel(const QrDesc<T>* __restrict__ descs) {
   const QrDesc<T>& D = descs[blockIdx.x];
   __shared__ double red[33];
@@ -57,9 +60,15 @@ __global__ void __launch_bounds__(kQrThreads) qr_kernel(const QrDesc<T>* __restr
       tr = (beta - ar) / beta;
       ti = -ai / beta;
       const cplx<double> den = mk<double>(ar - beta, ai);
-      for (int i = k + 1 + threadIdx.x; i < m; i += blockDim.x) {
-        const cplx<T> x = col[i];
-        col[i] = cdiv<T>(mk<double>((double)x.re, (double)x.im), den);
+      if (sizeof(Acc) == 8) {
+        for (int i = k + 1 + threadIdx.x; i < m; i += blockDim.x) {
+          const cplx<T> x = col[i];
+          col[i] = cdiv<T>(mk<double>((double)x.re, (double)x.im), den);
+        }
+      } else {
+        const double dd = den.re * den.re + den.im * den.im;
+        const cplx<T> inv = mk<T>((T)(den.re / dd), (T)(-den.im / dd));
+        for (int i = k + 1 + threadIdx.x; i < m; i += blockDim.x) col[i] = col[i] * inv;
       }
       __syncthreads();
       if (threadIdx.x == 0) col[k] = mk<T>((T)beta, (T)0);
@@ -74,18 +83,18 @@ __global__ void __launch_bounds__(kQrThreads) qr_kernel(const QrDesc<T>* __restr
       // trailing columns j > k: a_j -= conj(tau) v (v^H a_j)
       for (int j = k + 1 + wid; j < n; j += nw) {
         cplx<T>* aj = A + (long long)j * m;
-        double wr = 0.0, wi = 0.0;
+        Acc wr = 0, wi = 0;
         for (int i = k + lane; i < m; i += 32) {
           const cplx<T> v = i == k ? mk<T>(1, 0) : col[i];
           const cplx<T> a = aj[i];
-          wr += (double)v.re * a.re + (double)v.im * a.im;
-          wi += (double)v.re * a.im - (double)v.im * a.re;
+          wr += (Acc)v.re * a.re + (Acc)v.im * a.im;
+          wi += (Acc)v.re * a.im - (Acc)v.im * a.re;
         }
         wr = warp_sum(wr);
         wi = warp_sum(wi);
         // f = conj(tau) * w
-        const double fr = tr * wr + ti * wi;
-        const double fi = tr * wi - ti * wr;
+        const Acc fr = (Acc)tr * wr + (Acc)ti * wi;
+        const Acc fi = (Acc)tr * wi - (Acc)ti * wr;
         for (int i = k + lane; i < m; i += 32) {
           const cplx<T> v = i == k ? mk<T>(1, 0) : col[i];
           cplx<T> a = aj[i];
@@ -110,18 +119,18 @@ __global__ void __launch_bounds__(kQrThreads) qr_kernel(const QrDesc<T>* __restr
     const cplx<T>* col = A + (long long)k * m;
     for (int j = k + wid; j < qc; j += nw) {
       cplx<T>* qj = Q + (long long)j * m;
-      double wr = 0.0, wi = 0.0;
+      Acc wr = 0, wi = 0;
       for (int i = k + lane; i < m; i += 32) {
         const cplx<T> v = i == k ? mk<T>(1, 0) : col[i];
         const cplx<T> a = qj[i];
-        wr += (double)v.re * a.re + (double)v.im * a.im;
-        wi += (double)v.re * a.im - (double)v.im * a.re;
+        wr += (Acc)v.re * a.re + (Acc)v.im * a.im;
+        wi += (Acc)v.re * a.im - (Acc)v.im * a.re;
       }
       wr = warp_sum(wr);
       wi = warp_sum(wi);
       // H_k q = q - tau v (v^H q)
-      const double fr = tr * wr - ti * wi;
-      const double fi = tr * wi + ti * wr;
+      const Acc fr = (Acc)tr * wr - (Acc)ti * wi;
+      const Acc fi = (Acc)tr * wi + (Acc)ti * wr;
       for (int i = k + lane; i < m; i += 32) {
         const cplx<T> v = i == k ? mk<T>(1, 0) : col[i];
         cplx<T> a = qj[i];
@@ -155,14 +164,17 @@ __global__ void __launch_bounds__(kQrThreads) qr_kernel(const QrDesc<T>* __restr
 }  // namespace
 
 template <typename T>
-int launch_qr(const QrDesc<T>* d, int nd, cudaStream_t st) {
+int launch_qr(const QrDesc<T>* d, int nd, int gauge, cudaStream_t st) {
   if (nd <= 0) return QCA_OK;
-  qr_kernel<T><<<nd, kQrThreads, 0, st>>>(d);
+  if (gauge && sizeof(T) == 4)
+    qr_kernel<T, float><<<nd, kQrThreads, 0, st>>>(d);
+  else
+    qr_kernel<T, double><<<nd, kQrThreads, 0, st>>>(d);
   QCA_LAUNCH_CHECK();
   return QCA_OK;
 }
 
-template int launch_qr<double>(const QrDesc<double>*, int, cudaStream_t);
-template int launch_qr<float>(const QrDesc<float>*, int, cudaStream_t);
+template int launch_qr<double>(const QrDesc<double>*, int, int, cudaStream_t);
+template int launch_qr<float>(const QrDesc<float>*, int, int, cudaStream_t);
 
 }  // namespace qca

@@ -178,7 +178,8 @@ struct QrDesc {
 };
 
 template <typename T>
-int launch_qr(const QrDesc<T>* d, int nd, cudaStream_t st);
+// gauge != 0: a gauge move of the mixed path (FP32 sums); 0: FP64 sums
+int launch_qr(const QrDesc<T>* d, int nd, int gauge, cudaStream_t st);
 
 // ----------------------------------------------------------------------------------
 // elementwise helpers
