@@ -173,6 +173,13 @@ int qca_engine_kernel_stats(qca_engine* e, double* out, int reset);
  * mixed path; tensor_cores = 2 selects the 3xTF32 tcgen05 kernel, 1 the 3xTF32
  * mma.sync kernel, 0 the CUDA-core kernel.  Synchronises the stream. */
 int qca_test_gemm_c64(int M, int N, int K, const void* A, const void* B, void* C, int tensor_cores, void* stream);
+/* Test hook (no counterpart in the reference): the two-site split of 2TDVP alone
+ * (tdvp.py:286-296) on DEVICE arrays of the precision's complex type: theta (4, Dl,
+ * Dr) -> Al (2, Dl, k) = U and Ar (2, k, Dr) = s Vh / ||s|| with the truncation rule
+ * (eps, chi), sv (FP64, min(2 Dl, 2 Dr) values, descending), *k_out = k.  The
+ * output arrays need room for k = min(2 Dl, 2 Dr).  Synchronises the stream. */
+int qca_test_svd(int precision, int Dl, int Dr, const void* theta, int chi, double eps, void* Al, void* Ar,
+                 double* sv, int* k_out, void* stream);
 
 #ifdef __cplusplus
 }

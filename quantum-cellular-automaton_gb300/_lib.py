@@ -100,6 +100,7 @@ SIGNATURES = {
     "qca_engine_profile": [_P, _I],
     "qca_engine_kernel_stats": [_P, _PD, _I],
     "qca_test_gemm_c64": [_I, _I, _I, _P, _P, _P, _I, _P],
+    "qca_test_svd": [_I, _I, _I, _P, _I, _D, _P, _P, _P, _PI, _P],
 }
 
 _lib = None

@@ -29,6 +29,9 @@
 // in closed form by each rotation (a' = a - t|g|, b' = b + t|g|).
 #include <cooperative_groups.h>
 
+#include <algorithm>
+#include <cstring>
+
 #include "tdvp_kernels.cuh"
 
 namespace cg = cooperative_groups;
@@ -837,3 +840,75 @@ template int svd_cluster_size<double>(int, int);
 template int svd_cluster_size<float>(int, int);
 
 }  // namespace qca
+
+// Test hook: the two-site split on its own.  theta (4, Dl, Dr), Al (2, Dl, k) and
+// Ar (2, k, Dr) are DEVICE arrays of the precision's complex type with room for
+// k = min(2 Dl, 2 Dr); sv (device, FP64) receives the min(2 Dl, 2 Dr) singular
+// values in descending order; *k_out the truncated bond (right-sweep form: A_l = U,
+// A_r = s Vh / ||s||).  Synchronises the stream.
+template <typename T>
+static int test_svd(int Dl, int Dr, const void* theta, int chi, double eps, void* Al, void* Ar, double* sv,
+                    int* k_out, cudaStream_t st) {
+  using namespace qca;
+  const int m = 2 * Dl, n = 2 * Dr, mx = std::max(m, n), nx = std::min(m, n);
+  void* scratch = nullptr;
+  const size_t wbytes = sizeof(cplx<T>) * ((size_t)mx * nx + (size_t)nx * nx);
+  const size_t bytes = wbytes + 64 + sizeof(SvdDesc<T>);
+  QCA_CUDA(cudaMalloc(&scratch, bytes));
+  char* base = (char*)scratch;
+  SvdDesc<T> d;
+  memset(&d, 0, sizeof(d));
+  d.theta = (const cplx<T>*)theta;
+  d.Dl = Dl;
+  d.Dr = Dr;
+  d.chi = chi;
+  d.kmax = nx;
+  d.eps = eps;
+  d.right_sweep = 1;
+  d.Al = (cplx<T>*)Al;
+  d.Ar = (cplx<T>*)Ar;
+  d.work = (cplx<T>*)base;
+  d.sv = sv;
+  d.k_out = (int*)(base + wbytes);
+  d.status = (int*)(base + wbytes + 16);
+  d.discarded = (double*)(base + wbytes + 32);
+  SvdDesc<T>* dd = (SvdDesc<T>*)(base + wbytes + 64);
+  int s = QCA_OK;
+  int h[3] = {0, 0, 0};
+  if (cudaMemsetAsync(base + wbytes, 0, 64, st) != cudaSuccess ||
+      cudaMemcpyAsync(dd, &d, sizeof(d), cudaMemcpyHostToDevice, st) != cudaSuccess) {
+    set_error("qca_test_svd: %s", cudaGetErrorString(cudaGetLastError()));
+    s = QCA_ERR_CUDA;
+  }
+  if (s == QCA_OK) s = launch_svd<T>(dd, &d, 1, st);
+  if (s == QCA_OK && (cudaMemcpyAsync(h, base + wbytes, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                      cudaMemcpyAsync(h + 1, base + wbytes + 16, 2 * sizeof(int), cudaMemcpyDeviceToHost, st) !=
+                          cudaSuccess ||
+                      cudaStreamSynchronize(st) != cudaSuccess)) {
+    set_error("qca_test_svd: %s", cudaGetErrorString(cudaGetLastError()));
+    s = QCA_ERR_CUDA;
+  }
+  cudaFree(scratch);
+  if (s != QCA_OK) return s;
+  *k_out = h[0];
+  if (h[1] != 0) {
+    set_error("qca_test_svd: Jacobi sweeps did not converge (%d sweeps)", h[2]);
+    return QCA_ERR_NOT_CONVERGED;
+  }
+  return QCA_OK;
+}
+
+extern "C" int qca_test_svd(int precision, int Dl, int Dr, const void* theta, int chi, double eps, void* Al, void* Ar,
+                            double* sv, int* k_out, void* stream) {
+  using namespace qca;
+  if (Dl < 1 || Dr < 1 || 2 * std::min(Dl, Dr) > 1024 || 2 * std::max(Dl, Dr) > 512 || !theta || !Al || !Ar ||
+      !sv || !k_out || chi < 1 || !(eps >= 0)) {
+    set_error("qca_test_svd: invalid arguments");
+    return QCA_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  if (precision == QCA_PREC_FP64) return test_svd<double>(Dl, Dr, theta, chi, eps, Al, Ar, sv, k_out, st);
+  if (precision == QCA_PREC_MIXED) return test_svd<float>(Dl, Dr, theta, chi, eps, Al, Ar, sv, k_out, st);
+  set_error("qca_test_svd: unknown precision %d", precision);
+  return QCA_ERR_INVALID;
+}

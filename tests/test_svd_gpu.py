@@ -1,0 +1,85 @@
+"""The two-site split (one-sided Jacobi SVD on a thread-block cluster) on its
+own, against numpy's complex128 SVD of the same theta: singular values, the
+reconstruction A_l A_r = theta / ||theta||, the isometry of A_l, and the
+truncation rule (tdvp.py:286-296).  Sizes run from the 2 x 2 product-state split
+to 256 x 256 (bond dimension 128 on both sides), through both SVD kernels.
+Tolerances: FP64 1e-12; complex64 (mixed path) 2e-5 relative."""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [(1, 1), (1, 2), (2, 1), (3, 5), (17, 9), (16, 16), (40, 50), (64, 64), (100, 100), (128, 128), (130, 60)]
+
+
+def run_svd(prec, Dl, Dr, theta, chi=100000, eps=0.0):
+    import torch
+    from qca_gb300 import _lib
+    ct = torch.complex128 if prec == _lib.QCA_PREC_FP64 else torch.complex64
+    nx = 2 * min(Dl, Dr)
+    th = torch.from_numpy(theta).to(ct).cuda()
+    Al = torch.zeros(2 * Dl * nx, dtype=ct, device="cuda")
+    Ar = torch.zeros(2 * nx * Dr, dtype=ct, device="cuda")
+    sv = torch.zeros(nx, dtype=torch.float64, device="cuda")
+    k = ctypes.c_int(0)
+    torch.cuda.synchronize()
+    _lib.call("qca_test_svd", prec, Dl, Dr, ctypes.c_void_p(th.data_ptr()), chi, eps, ctypes.c_void_p(Al.data_ptr()),
+              ctypes.c_void_p(Ar.data_ptr()), ctypes.c_void_p(sv.data_ptr()), ctypes.byref(k), None)
+    kk = k.value
+    Al = Al[: 2 * Dl * kk].cpu().numpy().astype(np.complex128).reshape(2, Dl, kk)
+    Ar = Ar[: 2 * kk * Dr].cpu().numpy().astype(np.complex128).reshape(2, kk, Dr)
+    return Al, Ar, sv.cpu().numpy(), kk
+
+
+def theta_matrix(theta, Dl, Dr):
+    # Theta[(s1, a), (s2, c)] = theta[s1 * 2 + s2][a][c]
+    return theta.reshape(2, 2, Dl, Dr).transpose(0, 2, 1, 3).reshape(2 * Dl, 2 * Dr)
+
+
+@pytest.mark.parametrize("prec_name", ["fp64", "mixed"])
+@pytest.mark.parametrize("Dl,Dr", SIZES)
+def test_svd_matches_numpy(prec_name, Dl, Dr):
+    from qca_gb300 import _lib
+    prec = _lib.QCA_PREC_FP64 if prec_name == "fp64" else _lib.QCA_PREC_MIXED
+    if prec_name == "fp64" and max(Dl, Dr) > 64:
+        pytest.skip("FP64 SVD of this size runs on the slab kernel; covered up to bond 64")
+    tol = 1e-12 if prec_name == "fp64" else 2e-5
+    rng = np.random.default_rng(Dl * 1000 + Dr)
+    theta = rng.standard_normal((4, Dl, Dr)) + 1j * rng.standard_normal((4, Dl, Dr))
+    if prec_name == "mixed":
+        theta = theta.astype(np.complex64).astype(np.complex128)
+    M = theta_matrix(theta, Dl, Dr)
+    s_ref = np.linalg.svd(M, compute_uv=False)
+    Al, Ar, sv, k = run_svd(prec, Dl, Dr, theta)
+    nx = 2 * min(Dl, Dr)
+    assert k == nx
+    assert np.abs(sv - s_ref).max() <= tol * s_ref[0]
+    # A_l A_r = Theta / ||Theta||_F
+    R = np.einsum("sai,tic->satc", Al, Ar).reshape(2 * Dl, 2 * Dr)
+    assert np.abs(R - M / np.linalg.norm(M)).max() <= 10 * tol
+    U = Al.reshape(2 * Dl, k)
+    assert np.abs(U.conj().T @ U - np.eye(k)).max() <= 10 * tol
+
+
+@pytest.mark.parametrize("prec_name", ["fp64", "mixed"])
+def test_svd_truncation_rule(prec_name):
+    """k = min{i : ||s[i:]|| < eps} capped at chi, on a graded spectrum."""
+    from qca_gb300 import _lib
+    prec = _lib.QCA_PREC_FP64 if prec_name == "fp64" else _lib.QCA_PREC_MIXED
+    Dl = Dr = 12
+    rng = np.random.default_rng(5)
+    n = 2 * Dl
+    U, _ = np.linalg.qr(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    V, _ = np.linalg.qr(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    s = 10.0 ** (-0.5 * np.arange(n))
+    M = (U * s) @ V.conj().T
+    theta = M.reshape(2, Dl, 2, Dr).transpose(0, 2, 1, 3).reshape(4, Dl, Dr)
+    eps = 1e-3 * np.linalg.norm(s)
+    tail = np.sqrt(np.cumsum((s ** 2)[::-1])[::-1])
+    k_ref = int(np.argmax(tail < eps))
+    _, _, _, k = run_svd(prec, Dl, Dr, theta, eps=eps)
+    assert k == k_ref
+    _, _, _, k = run_svd(prec, Dl, Dr, theta, chi=3, eps=eps)
+    assert k == min(3, k_ref)
