@@ -3,7 +3,9 @@ own, against numpy's complex128 SVD of the same theta: singular values, the
 reconstruction A_l A_r = theta / ||theta||, the isometry of A_l, and the
 truncation rule (tdvp.py:286-296).  Sizes run from the 2 x 2 product-state split
 to 256 x 256 (bond dimension 128 on both sides), through both SVD kernels.
-Tolerances: FP64 1e-12; complex64 (mixed path) 2e-5 relative."""
+Tolerances: FP64 1e-12.  complex64 (mixed path): reconstruction and isometry
+2e-5; singular values 1e-4 relative to the largest, since each column carries the
+rounding of its few thousand FP32 rotations (about 2e-5 measured at 256 x 256)."""
 import ctypes
 
 import numpy as np
@@ -46,6 +48,7 @@ def test_svd_matches_numpy(prec_name, Dl, Dr):
     if prec_name == "fp64" and max(Dl, Dr) > 64:
         pytest.skip("FP64 SVD of this size runs on the slab kernel; covered up to bond 64")
     tol = 1e-12 if prec_name == "fp64" else 2e-5
+    tol_s = 1e-12 if prec_name == "fp64" else 1e-4
     rng = np.random.default_rng(Dl * 1000 + Dr)
     theta = rng.standard_normal((4, Dl, Dr)) + 1j * rng.standard_normal((4, Dl, Dr))
     if prec_name == "mixed":
@@ -55,12 +58,12 @@ def test_svd_matches_numpy(prec_name, Dl, Dr):
     Al, Ar, sv, k = run_svd(prec, Dl, Dr, theta)
     nx = 2 * min(Dl, Dr)
     assert k == nx
-    assert np.abs(sv - s_ref).max() <= tol * s_ref[0]
+    assert np.abs(sv - s_ref).max() <= tol_s * s_ref[0]
     # A_l A_r = Theta / ||Theta||_F
     R = np.einsum("sai,tic->satc", Al, Ar).reshape(2 * Dl, 2 * Dr)
-    assert np.abs(R - M / np.linalg.norm(M)).max() <= 10 * tol
+    assert np.abs(R - M / np.linalg.norm(M)).max() <= tol
     U = Al.reshape(2 * Dl, k)
-    assert np.abs(U.conj().T @ U - np.eye(k)).max() <= 10 * tol
+    assert np.abs(U.conj().T @ U - np.eye(k)).max() <= tol
 
 
 @pytest.mark.parametrize("prec_name", ["fp64", "mixed"])
@@ -76,7 +79,7 @@ def test_svd_truncation_rule(prec_name):
     s = 10.0 ** (-0.5 * np.arange(n))
     M = (U * s) @ V.conj().T
     theta = M.reshape(2, Dl, 2, Dr).transpose(0, 2, 1, 3).reshape(4, Dl, Dr)
-    eps = 1e-3 * np.linalg.norm(s)
+    eps = 0.5e-3 * np.linalg.norm(s)  # between the tails at i = 6 and 7, clear of both
     tail = np.sqrt(np.cumsum((s ** 2)[::-1])[::-1])
     k_ref = int(np.argmax(tail < eps))
     _, _, _, k = run_svd(prec, Dl, Dr, theta, eps=eps)
