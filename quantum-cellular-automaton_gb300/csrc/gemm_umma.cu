@@ -145,8 +145,25 @@ struct UmCur {
   int tile, s;
 };
 
-__device__ __forceinline__ bool um_tile(const GemmDesc<float>* descs, int nd, int tile, UmTile& T) {
-  const GemmDesc<float>* D = descs + um_find_desc(descs, nd, tile);
+// first tiles of the problems, staged in shared memory for the tile lookups of a
+// persistent CTA (a binary search over global memory is a chain of dependent loads)
+constexpr int kUmMaxDesc = 2048;
+
+__device__ __forceinline__ int um_find_tile(const int* tb, const GemmDesc<float>* d, int nd, int tile) {
+  if (nd > kUmMaxDesc) return um_find_desc(d, nd, tile);
+  int lo = 0, hi = nd - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tb[mid] <= tile)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ bool um_tile(const int* tb, const GemmDesc<float>* descs, int nd, int tile, UmTile& T) {
+  const GemmDesc<float>* D = descs + um_find_tile(tb, descs, nd, tile);
   if (D->skip && *D->skip) return false;
   int t = tile - D->tile_begin;
   const int per_batch = D->tiles_m * D->tiles_n;
@@ -167,9 +184,10 @@ __device__ __forceinline__ bool um_tile(const GemmDesc<float>* descs, int nd, in
 }
 
 // first valid tile at or after `from` in this CTA's stride
-__device__ __forceinline__ void um_seek(const GemmDesc<float>* descs, int nd, int total, int from, UmCur& c) {
+__device__ __forceinline__ void um_seek(const int* tb, const GemmDesc<float>* descs, int nd, int total, int from,
+                                        UmCur& c) {
   for (int t = from; t < total; t += gridDim.x)
-    if (um_tile(descs, nd, t, c.T)) {
+    if (um_tile(tb, descs, nd, t, c.T)) {
       c.tile = t;
       c.s = 0;
       return;
@@ -178,13 +196,13 @@ __device__ __forceinline__ void um_seek(const GemmDesc<float>* descs, int nd, in
   c.s = -1;
 }
 
-__device__ __forceinline__ void um_advance(const GemmDesc<float>* descs, int nd, int total, UmCur& c) {
+__device__ __forceinline__ void um_advance(const int* tb, const GemmDesc<float>* descs, int nd, int total, UmCur& c) {
   if (c.s < 0) return;
   if (c.s + 1 < c.T.nst) {
     ++c.s;
     return;
   }
-  um_seek(descs, nd, total, c.tile + gridDim.x, c);
+  um_seek(tb, descs, nd, total, c.tile + gridDim.x, c);
 }
 
 // Persistent: CTA b takes tiles b, b + gridDim.x, ...; the stage pipeline runs on
@@ -195,8 +213,12 @@ __global__ void __launch_bounds__(kUmThreads, 1) gemm_umma_grouped(const GemmDes
   extern __shared__ __align__(16) unsigned char um_raw[];
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t tslot;
+  __shared__ int s_tb[kUmMaxDesc];
+  if (nd <= kUmMaxDesc)
+    for (int i = threadIdx.x; i < nd; i += blockDim.x) s_tb[i] = descs[i].tile_begin;
+  __syncthreads();
   UmCur F;  // next stage to fetch from global memory
-  um_seek(descs, nd, total, blockIdx.x, F);
+  um_seek(s_tb, descs, nd, total, blockIdx.x, F);
   if (F.s < 0) return;  // no work for this CTA (uniform)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   // operand planes of buffer b: sbase + b * kUmStage + p * kUmPlane (p: A hi, A lo, B hi, B lo)
@@ -336,7 +358,7 @@ __global__ void __launch_bounds__(kUmThreads, 1) gemm_umma_grouped(const GemmDes
 
   UmCur S = F;  // stage to stash and multiply
   fetch(F);
-  um_advance(descs, nd, total, F);
+  um_advance(s_tb, descs, nd, total, F);
   UmCur R;  // stage to read out (previous iteration's)
   R.s = -1;
   int g = 0;
@@ -371,7 +393,7 @@ __global__ void __launch_bounds__(kUmThreads, 1) gemm_umma_grouped(const GemmDes
     }
     R = S;
     S = F;
-    um_advance(descs, nd, total, F);
+    um_advance(s_tb, descs, nd, total, F);
   }
   // the last stage issued (R, global index g - 1) ends the CTA's last tile
   if (ok) readout(g - 1);
