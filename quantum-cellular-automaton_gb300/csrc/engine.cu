@@ -386,11 +386,11 @@ struct Engine final : EngineBase {
       QCA_TRY(upload(v, st, &dd));
       return timed(KC_GEMM, fl, by, st, [&] { return launch_gemm<T>(dd, v.data(), (int)v.size(), cfg, st); });
     }
-    // mixed path: 3xTF32 on the tensor cores.  Problems that fill the tcgen05 tile
-    // (M >= kUmmaMinM, N and K >= kUmmaMinNK: 128 x 64 tiles, 16-deep K stages) go to
-    // the tcgen05 kernel, the others to the mma.sync kernel (64 x 64); the choice
-    // depends on the problem's own shape only, so a chain's arithmetic does not depend
-    // on which other chains share the launch.
+    // mixed path: 3xTF32 on the tensor cores.  Problems with M >= kUmmaMinM and N,
+    // K >= kUmmaMinNK go to the tcgen05 kernel (128 x 64 tiles, 16-deep K stages),
+    // the others to the mma.sync kernel (64 x 64); the choice depends on the
+    // problem's own shape only, so a chain's arithmetic does not depend on which
+    // other chains share the launch.
     std::vector<GemmDesc<T>> big, small;
     for (auto& d : v)
       (use_umma && d.M >= kUmmaMinM && d.N >= kUmmaMinNK && (long long)d.K * d.G >= kUmmaMinNK ? big : small)

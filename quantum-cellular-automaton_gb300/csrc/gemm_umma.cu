@@ -1,8 +1,8 @@
 // Grouped complex64 GEMM on the fifth-generation tensor cores: tcgen05.mma
 // kind::tf32 with the accumulators in tensor memory (TMEM), 3xTF32 split precision.
-// Used by the mixed-precision path for the TDVP contractions that fill its tile
-// (M >= 96, N and K >= 64: environment updates and the effective-Hamiltonian
-// stages, tdvp.py:298-347).
+// Used by the mixed-precision path for the TDVP contractions with M >= 48 and
+// N, K >= 32 (environment updates and the effective-Hamiltonian stages,
+// tdvp.py:298-347).
 //
 // The complex product is one real GEMM over an embedding that doubles K and N
 // (per K stage of BK complex elements and per 64-column tile):

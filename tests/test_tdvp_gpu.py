@@ -146,10 +146,12 @@ def test_tdvp_mixed_tracks_fp64_at_large_bonds(alg_name):
     """A random MPS with bonds up to 48 (local problems with M = 4 D >= 96 take the
     tcgen05 contraction kernel): two mixed-precision steps agree with the FP64
     path (itself pinned to the reference).  The bond cap (96) is above what two
-    steps reach.  Tolerance 3e-5: on this random, highly entangled state the mixed
-    path differs from FP64 by 1.4e-5 (2TDVP) and 1.7e-5 (1TDVP) after two steps,
-    the same with the tcgen05, the mma.sync and the FP32 CUDA-core contraction
-    kernels, i.e. set by the FP32 storage of the state, not by the GEMM."""
+    steps reach.  On this random, highly entangled state the mixed 2TDVP differs
+    from FP64 by 1.4e-5 after two steps with the tcgen05, the mma.sync and the FP32
+    CUDA-core contraction kernels alike (set by the FP32 storage of the state):
+    tolerance 3e-5.  1TDVP grows bonds from the complement columns of nearly
+    rank-deficient complete QRs, which amplify contraction rounding (1e-6 to 3e-5
+    depending on the kernel): tolerance 5e-5, as for its golden fixtures."""
     from qca_gb300 import GpuTDVP, MPO, MPS, Rules
     n, d, lo, hi, dt, chi = 14, 2, 2, 4, 0.05, 96
     rng = np.random.default_rng(77)
@@ -170,5 +172,5 @@ def test_tdvp_mixed_tracks_fp64_at_large_bonds(alg_name):
         r = rows(n)
         alg.measure(*r)
         res.append(r)
-    assert np.abs(res[0][0] - res[1][0]).max() < 3e-5
+    assert np.abs(res[0][0] - res[1][0]).max() < (3e-5 if alg_name == "2tdvp" else TOL_MIXED_1TDVP)
 
