@@ -278,10 +278,15 @@ def run_tdvp(args, dist: Dist):
     launches = int(sum(v["launches"] for v in ks.values()))
     gemm = ks["gemm"]
     tflops = gemm["flops"] / (gemm["ms"] / 1e3) / 1e12 if gemm["ms"] > 0 else 0.0
-    roofline = {"kernel": dom, "bound": "tensor",
+    svd = ks["svd"]
+    svd_tflops = svd["flops"] / (svd["ms"] / 1e3) / 1e12 if svd["ms"] > 0 else 0.0
+    # the tensor-core contraction class carries the roofline (tensor-bound); the SVD
+    # class (FP32 CUDA cores, latency of its rotation rounds) is reported beside it
+    roofline = {"kernel": "gemm", "dominant_class": dom, "bound": "tensor",
                 "achieved": round(tflops, 3), "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
                 "frac": round(tflops / pk["bf16_tflops"], 5), "traffic": None,
                 "peak_source": f"{pk['source']} bf16 dense", "measured_kernel": "gemm",
+                "svd_achieved_tflops_fp32": round(svd_tflops, 3),
                 "kernel_time_share": {k: round(v["ms"] / max(1e-9, sum(x["ms"] for x in ks.values())), 4)
                                       for k, v in ks.items()},
                 "kernel_ms_per_step": round(sum(x["ms"] for x in ks.values()) / args.steps, 3)}
