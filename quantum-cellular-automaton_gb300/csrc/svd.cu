@@ -90,32 +90,32 @@ struct DF {
   __device__ __forceinline__ float value() const { return hi + lo; }
 };
 
-// Warp-wide sums over the RPL elements each lane holds.  In FP32 the sums are
-// compensated (each product split exactly with an FMA, partial sums carried as
-// hi + lo pairs, also through the warp reduction), so that small inner products of
-// nearly orthogonal columns are resolved beyond the sqrt(m) eps32 noise of a plain
-// FP32 sum and the rotations can drive the columns to FP32-level orthogonality.
-// Every lane returns lane 0's result, so that all lanes of a warp take the same
-// branch and apply the same rotation.
+// Warp-wide sums over the RPL elements each lane holds: the pair's inner product in
+// the working precision (each lane sums at most 16 elements, then a 5-level tree,
+// which keeps the FP32 error at a few eps32 |u||v|, below the FP32 rotation
+// tolerance of 16 eps32); the squared column norms compensated in FP32 (products
+// split exactly with an FMA, partial sums carried as hi + lo pairs, also through the
+// warp reduction).  Every lane returns lane 0's result, so that all lanes of a warp
+// take the same branch and apply the same rotation.
 template <typename T, int RPL>
 __device__ __forceinline__ void pair_cross(const cplx<T> (&ru)[RPL], const cplx<T> (&rv)[RPL], T& gr, T& gi) {
   if constexpr (sizeof(T) == 4) {
-    DF r, i;
+    // plain FP32: each lane sums only RPL <= 16 elements, then a 5-level tree, so
+    // the error stays a few eps32 |u||v|, below the rotation tolerance of 16 eps32
+    float r = 0.f, i = 0.f;
 #pragma unroll
     for (int k = 0; k < RPL; ++k) {
       const cplx<T> u = ru[k], v = rv[k];
-      r.add_prod(u.re, v.re);  // conj(u) v
-      r.add_prod(u.im, v.im);
-      i.add_prod(u.re, v.im);
-      i.add_prod(-u.im, v.re);
+      r = fmaf(u.re, v.re, fmaf(u.im, v.im, r));  // conj(u) v
+      i = fmaf(u.re, v.im, fmaf(-u.im, v.re, i));
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      r.add_df(__shfl_xor_sync(0xffffffffu, r.hi, o), __shfl_xor_sync(0xffffffffu, r.lo, o));
-      i.add_df(__shfl_xor_sync(0xffffffffu, i.hi, o), __shfl_xor_sync(0xffffffffu, i.lo, o));
+      r += __shfl_xor_sync(0xffffffffu, r, o);
+      i += __shfl_xor_sync(0xffffffffu, i, o);
     }
-    gr = r.value();
-    gi = i.value();
+    gr = r;
+    gi = i;
   } else {
     T r = 0, i = 0;
 #pragma unroll
@@ -420,7 +420,7 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
   const double fro = *cluster.map_shared_rank(&s_fro, 0);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int P = nx + (nx & 1);
-  const double tol = Prec<T>::eps * (sizeof(T) == 4 ? 8.0 : fmax(8.0, 2.0 * sqrt((double)mx)));
+  const double tol = Prec<T>::eps * (sizeof(T) == 4 ? 16.0 : fmax(8.0, 2.0 * sqrt((double)mx)));
   const T floor2 = (T)(16.0 * Prec<T>::eps * Prec<T>::eps * fro);
   int* flag0 = cluster.map_shared_rank(s_flag, 0);
   int sweep = 0;
@@ -552,7 +552,7 @@ __global__ void __launch_bounds__(kSvdThreads) svd_block_kernel(const SvdDesc<T>
   cluster.sync();
   const double fro = *cluster.map_shared_rank(&s_fro, 0);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const double tol = Prec<T>::eps * (sizeof(T) == 4 ? 8.0 : fmax(8.0, 2.0 * sqrt((double)mx)));
+  const double tol = Prec<T>::eps * (sizeof(T) == 4 ? 16.0 : fmax(8.0, 2.0 * sqrt((double)mx)));
   const T floor2 = (T)(16.0 * Prec<T>::eps * Prec<T>::eps * fro);
   int* flag0 = cluster.map_shared_rank(s_flag, 0);
   int gen = 0, sweep = 0;
