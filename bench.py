@@ -543,14 +543,14 @@ def run_serving(args, dist: Dist):
     from qca_gb300.serving import Server
     torch.cuda.set_device(dist.local)
     jobs = W.poisson_jobs(rate=200.0, duration=60.0, seed=7 + dist.rank)
-    srv = Server(args.precision, hbm_budget_bytes=150 << 30, stream_every=10, max_resident=args.chains)
+    srv = Server(args.precision, hbm_budget_bytes=150 << 30, stream_every=10, max_resident=args.chains, group=16)
     rep = srv.run(jobs, time_limit=args.serve_seconds)
     return {"metric": "site-updates/s", "value": round(rep["site_updates_per_s"], 1), "unit": "site-updates/s",
             "n_gpus": dist.world, "higher_is_better": True, "data": "synthetic",
             "config": {"workload": "serving: Poisson 200/s over 60 s, 1TDVP/2TDVP, N~U{12..128}, d in {1,2}, "
                                    "chi in {16..256}, 50-500 steps, dt=0.05, HBM budget 150 GB",
                        "wall_limit_s": args.serve_seconds, "precision": args.precision,
-                       "max_resident_jobs": args.chains,
+                       "max_resident_jobs": args.chains, "jobs_per_engine_call": 16,
                        "jobs_in_trace": len(jobs)},
             "p50_latency_s": rep["p50_latency_s"], "p99_latency_s": rep["p99_latency_s"],
             "p50_step_round_s": rep["p50_round_s"], "p99_step_round_s": rep["p99_round_s"],

@@ -7,7 +7,10 @@ the HBM budget.  Every scheduling round advances every resident job by one
 time step in the same grouped launches (the engine's lock-step ticks), so jobs
 that arrive while others run join the next round and their work overlaps on
 the device.  <n_i> is streamed back every ``stream_every`` steps and at the end
-of each job through ``on_populations(job_id, step, populations)``.
+of each job through ``on_populations(job_id, step, populations)``.  A round steps
+the resident jobs in groups of at most ``group`` (one engine call each); with a
+deadline, the groups left when it passes wait for the next round, so a bounded
+run overruns its wall time by at most one group step.
 
 This replaces the reference's per-state driver loop (``quantum_game.py:28-119``:
 one initial state at a time, measure every plot interval) with a multi-job
@@ -42,13 +45,14 @@ class JobState:
 
 class Server:
     def __init__(self, precision: str = "mixed", hbm_budget_bytes: int = 150 << 30, stream_every: int = 10,
-                 max_resident: int = 512, on_populations=None) -> None:
+                 max_resident: int = 512, on_populations=None, group: int | None = None) -> None:
         self.precision = _lib.QCA_PREC_MIXED if precision == "mixed" else _lib.QCA_PREC_FP64
         self.engine = _Engine(self.precision, hbm_budget_bytes)
         self.budget = hbm_budget_bytes
         self.used = 0
         self.stream_every = stream_every
         self.max_resident = max_resident
+        self.group = group if group is not None else max_resident
         self.on_populations = on_populations
         self.pending: deque[JobState] = deque()
         self.active: list[JobState] = []
@@ -108,20 +112,27 @@ class Server:
                 self.on_populations(j.job_id, j.steps_done, p)
 
     # ------------------------------------------------------------------ loop
-    def round(self, now: float | None = None) -> bool:
-        """Admit what has arrived, advance every resident job by one step,
-        stream populations, retire finished jobs.  Returns False when idle."""
+    def round(self, now: float | None = None, deadline: float | None = None) -> bool:
+        """Admit what has arrived, advance the resident jobs by one step (group by
+        group, until ``deadline``), stream populations, retire finished jobs.
+        Returns False when idle."""
         now = time.perf_counter() if now is None else now
         t_round = time.perf_counter()
         self._admit(now)
         if not self.active:
             return bool(self.pending)
-        ids = (ctypes.c_int * len(self.active))(*[j.chain for j in self.active])
-        _lib.call("qca_engine_step_chains", self.engine.h, ids, len(self.active), 1, None)
-        for j in self.active:
-            j.steps_done += 1
-            self.site_updates += j.spec.site_updates_per_step()
-        due = [j for j in self.active if j.steps_done % self.stream_every == 0 or j.steps_done >= j.spec.steps]
+        stepped = []
+        for g0 in range(0, len(self.active), max(1, self.group)):
+            if deadline is not None and time.perf_counter() > deadline:
+                break
+            grp = self.active[g0:g0 + max(1, self.group)]
+            ids = (ctypes.c_int * len(grp))(*[j.chain for j in grp])
+            _lib.call("qca_engine_step_chains", self.engine.h, ids, len(grp), 1, None)
+            for j in grp:
+                j.steps_done += 1
+                self.site_updates += j.spec.site_updates_per_step()
+            stepped += grp
+        due = [j for j in stepped if j.steps_done % self.stream_every == 0 or j.steps_done >= j.spec.steps]
         self._measure(due)
         t = time.perf_counter()
         self.round_times.append(t - t_round)
@@ -152,7 +163,8 @@ class Server:
             if not self.active and self.pending and self.pending[0].arrival > now:
                 time.sleep(min(0.01, self.pending[0].arrival - now))
             # no admissions that would start after the time limit
-            self.round(now if time_limit is None or now - t0 < time_limit else t0)
+            self.round(now if time_limit is None or now - t0 < time_limit else t0,
+                       None if time_limit is None else t0 + time_limit)
         elapsed = time.perf_counter() - t0
         return self.report(elapsed)
 

@@ -122,3 +122,43 @@ def test_poisson_trace_shape():
     assert 300 < len(jobs) < 500
     assert all(12 <= j.spec.n <= 128 and j.spec.distance in (1, 2) for j in jobs)
     assert all(50 <= j.spec.steps <= 500 for j in jobs)
+
+
+def test_serving_round_stops_at_its_deadline(monkeypatch):
+    """The serving loop's host logic with the engine faked: a round steps the
+    resident jobs group by group and leaves the groups after its deadline for the
+    next round; a bounded run overruns its wall time by at most one group step."""
+    from qca_gb300 import serving
+    from qca_gb300.workloads import ChainSpec
+    clock = {"t": 0.0}
+    stepped = []
+
+    class FakeEngine:
+        def __init__(self, *a, **k):
+            self.h = ctypes.c_void_p(1)
+
+    def fake_call(name, *args):
+        if name == "qca_chain_footprint":
+            args[2]._obj.value = 1000
+        elif name == "qca_chain_add":
+            fake_call.next_id += 1
+            args[3]._obj.value = fake_call.next_id
+        elif name == "qca_engine_step_chains":
+            stepped.append(args[2])
+            clock["t"] += 1.0  # every engine call takes one second
+    fake_call.next_id = 0
+    monkeypatch.setattr(serving, "_Engine", FakeEngine)
+    monkeypatch.setattr(serving._lib, "call", fake_call)
+    monkeypatch.setattr(serving.time, "perf_counter", lambda: clock["t"])
+    monkeypatch.setattr(serving.time, "sleep", lambda s: clock.__setitem__("t", clock["t"] + s))
+    spec = ChainSpec(n=6, distance=1, interval=range(1, 2), chi=4, p=np.full(6, 0.5), steps=100)
+    srv = serving.Server("mixed", hbm_budget_bytes=1 << 30, stream_every=1000, max_resident=5, group=2)
+    for _ in range(5):
+        srv.submit(spec, arrival=0.0)
+    srv.round(now=0.0, deadline=0.5)  # first group runs, then the deadline has passed
+    assert stepped == [2]
+    assert [j.steps_done for j in srv.active] == [1, 1, 0, 0, 0]
+    srv.round(now=1.0)  # no deadline: every group
+    assert stepped == [2, 2, 2, 1]
+    rep = srv.run([], time_limit=2.5)  # 2 groups fit, the third starts after the limit
+    assert rep["elapsed_s"] <= 2.5 + 1.0
