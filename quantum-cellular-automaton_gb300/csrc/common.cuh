@@ -92,6 +92,19 @@ __host__ __device__ __forceinline__ void cfma_conj(cplx<T>& acc, cplx<T> a, cplx
 }
 
 // ----------------------------------------------------------------------------------
+// Slot of the current device in per-device caches of one-time launch set-up
+// (function attributes are per device); -1 when it cannot be used, and the caller
+// then sets up on every launch.
+constexpr int kMaxDevices = 64;
+inline int device_slot() {
+  int d = -1;
+  if (cudaGetDevice(&d) != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  return d >= 0 && d < kMaxDevices ? d : -1;
+}
+
 // warp / block reductions in double precision
 // ----------------------------------------------------------------------------------
 __device__ __forceinline__ float warp_sum(float v) {

@@ -377,10 +377,11 @@ int launch_gemm_tc(const GemmDesc<float>* d_desc, const GemmDesc<float>* h_desc,
   const GemmDesc<float>& last = h_desc[ndesc - 1];
   const int tiles = last.tile_begin + last.nb1 * last.nb2 * last.tiles_m * last.tiles_n;
   if (tiles <= 0) return QCA_OK;
-  static bool configured = false;
-  if (!configured) {
+  static bool configured[kMaxDevices] = {};
+  const int dv = device_slot();
+  if (dv < 0 || !configured[dv]) {
     QCA_CUDA(cudaFuncSetAttribute(gemm_tc_grouped, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * sizeof(TcSmem)));
-    configured = true;
+    if (dv >= 0) configured[dv] = true;
   }
   gemm_tc_grouped<<<tiles, 256, 2 * sizeof(TcSmem), st>>>(d_desc, ndesc);
   QCA_LAUNCH_CHECK();

@@ -414,12 +414,15 @@ int launch_gemm_umma(const GemmDesc<float>* d_desc, const GemmDesc<float>* h_des
   const GemmDesc<float>& last = h_desc[ndesc - 1];
   const int tiles = last.tile_begin + last.nb1 * last.nb2 * last.tiles_m * last.tiles_n;
   if (tiles <= 0) return QCA_OK;
-  static int sms = 0;
+  static int sm_count[kMaxDevices] = {};
+  const int dv = device_slot();
+  int sms = dv >= 0 ? sm_count[dv] : 0;
   if (!sms) {
     QCA_CUDA(cudaFuncSetAttribute(gemm_umma_grouped, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kUmSmem));
     int dev = 0;
     QCA_CUDA(cudaGetDevice(&dev));
     QCA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    if (dv >= 0) sm_count[dv] = sms;
   }
   // persistent: one CTA per SM (shared memory and registers admit one)
   const int grid = tiles < sms ? tiles : sms;

@@ -796,13 +796,14 @@ int launch_svd(const SvdDesc<T>* d, const SvdDesc<T>* h, int nd, cudaStream_t st
   size_t smem = 0;
   if (svd_block_plan<T>(mxmax, nxmax, &P, &b, &smem, &vs)) {
     // column length <= 256: RPL <= 8
-    static bool configured[2][3] = {};
+    static bool configured[kMaxDevices][2][3] = {};
+    const int dv = device_slot();
     void (*kern)(const SvdDesc<T>*, int, int) =
         rpl == 2 ? svd_block_kernel<T, 2> : rpl == 4 ? svd_block_kernel<T, 4> : svd_block_kernel<T, 8>;
-    if (!configured[ti][ri]) {
+    if (dv < 0 || !configured[dv][ti][ri]) {
       QCA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSvdSmem));
       QCA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-      configured[ti][ri] = true;
+      if (dv >= 0) configured[dv][ti][ri] = true;
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(nd * P, 1, 1);
@@ -824,11 +825,13 @@ int launch_svd(const SvdDesc<T>* d, const SvdDesc<T>* h, int nd, cudaStream_t st
     set_error("SVD of %d x %d exceeds the distributed shared memory of a 16-CTA cluster", mxmax, nxmax);
     return QCA_ERR_INVALID;
   }
-  static bool configured[2][4] = {};
+  static bool configured[kMaxDevices][2][4] = {};
+  const int dv = device_slot();
+  bool once = false;
   void (*kern)(const SvdDesc<T>*, int, int, int) =
       rpl == 2 ? svd_cluster_kernel<T, 2>
                : rpl == 4 ? svd_cluster_kernel<T, 4> : rpl == 8 ? svd_cluster_kernel<T, 8> : svd_cluster_kernel<T, 16>;
-  QCA_TRY(configure<T>(kern, &configured[ti][ri]));
+  QCA_TRY(configure<T>(kern, dv >= 0 ? &configured[dv][ti][ri] : &once));
   return launch_cluster<T>(kern, d, nd, cs, cpc, vs, smem, st);
 }
 
