@@ -1404,7 +1404,7 @@ struct Engine final : EngineBase {
     QCA_TRY(sync(st));
     if (std::is_same<T, float>::value && use_tc && use_umma) {
       int timeouts = 0;
-      QCA_TRY(gemm_umma_timeouts(1, &timeouts));
+      QCA_TRY(gemm_umma_timeouts(1, &timeouts, st));
       if (timeouts) {
         set_error("tensor-core GEMM: %d mbarrier waits ran out", timeouts);
         return QCA_ERR_CUDA;

@@ -436,7 +436,7 @@ extern "C" int qca_test_gemm_c64(int M, int N, int K, const void* A, const void*
   QCA_CUDA(cudaStreamSynchronize(st));
   if (um) {
     int timeouts = 0;
-    QCA_TRY(gemm_umma_timeouts(1, &timeouts));
+    QCA_TRY(gemm_umma_timeouts(1, &timeouts, st));
     if (timeouts) {
       set_error("qca_test_gemm_c64: %d tensor-core mbarrier waits ran out", timeouts);
       return QCA_ERR_CUDA;

@@ -431,11 +431,13 @@ int launch_gemm_umma(const GemmDesc<float>* d_desc, const GemmDesc<float>* h_des
   return QCA_OK;
 }
 
-int gemm_umma_timeouts(int reset, int* count) {
-  QCA_CUDA(cudaMemcpyFromSymbol(count, g_umma_timeouts, sizeof(int)));
+int gemm_umma_timeouts(int reset, int* count, cudaStream_t st) {
+  QCA_CUDA(cudaMemcpyFromSymbolAsync(count, g_umma_timeouts, sizeof(int), 0, cudaMemcpyDeviceToHost, st));
+  QCA_CUDA(cudaStreamSynchronize(st));
   if (reset && *count) {
     const int z = 0;
-    QCA_CUDA(cudaMemcpyToSymbol(g_umma_timeouts, &z, sizeof(int)));
+    QCA_CUDA(cudaMemcpyToSymbolAsync(g_umma_timeouts, &z, sizeof(int), 0, cudaMemcpyHostToDevice, st));
+    QCA_CUDA(cudaStreamSynchronize(st));
   }
   return QCA_OK;
 }

@@ -42,8 +42,9 @@ int launch_gemm_tc(const GemmDesc<float>* d_desc, const GemmDesc<float>* h_desc,
 // whose per-k8 FP32 accumulation 1TDVP's rank-deficient QRs prefer.
 constexpr int kUmmaBM = 128, kUmmaBN = 64, kUmmaMinM = 48, kUmmaMinNK = 32;
 int launch_gemm_umma(const GemmDesc<float>* d_desc, const GemmDesc<float>* h_desc, int ndesc, cudaStream_t st);
-// number of tensor-core GEMM mbarrier waits that ran out since the last reset
-int gemm_umma_timeouts(int reset, int* count);
+// number of tensor-core GEMM mbarrier waits that ran out since the last reset (read
+// in order on stream st)
+int gemm_umma_timeouts(int reset, int* count, cudaStream_t st);
 
 // Tile configuration for a set of problems (0: 16x16, 1: 32x32, 2: 64x64).
 int gemm_tile_cfg(int maxM, int maxN);
