@@ -13,8 +13,9 @@
 // and each real product x y is evaluated as xh yh + xh yl + xl yh from the TF32
 // parts xh = tf32(x), xl = tf32(x - xh).
 //
-// One CTA (256 threads) computes a 128 x 64 complex tile (128 x 128 real
-// accumulators).  Per K stage of 16 complex elements all threads convert the
+// A CTA (256 threads) computes 128 x 64 complex tiles (128 x 128 real accumulators);
+// the kernel is persistent, one CTA per SM walking the tiles b, b + grid, ..., and
+// its stage pipeline runs on across tile boundaries.  Per K stage of 16 complex elements all threads convert the
 // stage's operands and store them in shared memory in the canonical K-major layout
 // without swizzle (core matrices of 8 rows x 16 bytes): a thread owns one row and
 // four consecutive K elements and writes whole 16-byte core-matrix rows, lanes on
