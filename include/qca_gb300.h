@@ -140,14 +140,17 @@ int qca_chain_remove(qca_engine* e, int chain_id);
 int qca_engine_step(qca_engine* e, int nsteps, void* stream);
 /* do_time_step nsteps times for the listed chains only (the others keep their state). */
 int qca_engine_step_chains(qca_engine* e, const int* chain_ids, int count, int nsteps, void* stream);
-/* Algorithm.measure (algorithm.py:58-63 -> mps.py:100-140).  Mutates the gauge of the
- * stored MPS exactly like the reference.  Outputs: population[N], d_population[N],
- * single_site_entropy[N], bond_dims[N+1] (any may be NULL). */
+/* Algorithm.measure (algorithm.py:58-63 -> mps.py:100-140).  1TDVP chains: mutates
+ * the gauge of the stored MPS exactly like the reference.  2TDVP chains whose
+ * orthogonality centre is at site 0 (the state after every step): the same left QR
+ * sweep runs on scratch copies, which gives the same values without touching the
+ * tensors (the result does not depend on the gauge).  Outputs: population[N],
+ * d_population[N], single_site_entropy[N], bond_dims[N+1] (any may be NULL). */
 int qca_chain_measure(qca_engine* e, int chain_id, double* population, double* d_population,
                       double* single_site_entropy, double* bond_dims, void* stream);
 /* Algorithm.measure for `count` chains at once (their QR sweeps run in lock step);
  * the outputs are concatenated over the chains in the given order: N_c values per
- * chain (N_c + 1 for bond_dims).  Mutates the gauges like qca_chain_measure. */
+ * chain (N_c + 1 for bond_dims).  Gauges as in qca_chain_measure. */
 int qca_engine_measure(qca_engine* e, const int* chain_ids, int count, double* population, double* d_population,
                        double* single_site_entropy, double* bond_dims, void* stream);
 /* Current MPS bond dimensions D_0..D_N. */
