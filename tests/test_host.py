@@ -162,3 +162,35 @@ def test_serving_round_stops_at_its_deadline(monkeypatch):
     assert stepped == [2, 2, 2, 1]
     rep = srv.run([], time_limit=2.5)  # 2 groups fit, the third starts after the limit
     assert rep["elapsed_s"] <= 2.5 + 1.0
+
+
+def test_bench_roofline_arithmetic():
+    """bench.py's roofline object from per-class kernel statistics (the numbers of
+    a recorded batched run): the GEMM class against the measured bf16 peak, the
+    derived 3xTF32 ceiling, the whole-step rate, shares that sum to one, and a
+    line that serialises to JSON."""
+    import json
+    import sys
+    sys.path.insert(0, ROOT)
+    import bench
+    ms = 3 * 3476.8
+    ks = {k: {"launches": 1000.0, "ms": 0.0, "flops": 0.0, "bytes": 0.0} for k in bench.KCLASS}
+    ks["gemm"].update(ms=4373.0, flops=16.92e12 * 4.373)
+    ks["svd"].update(ms=3387.0, flops=0.653e12 * 3.387)
+    ks["lanczos_vec"].update(ms=880.0)
+    ks["mpo_apply"].update(ms=584.0)
+    ks["lanczos_exp"].update(ms=317.0)
+    pk = {"hbm_gbs": 6800.3, "bf16_tflops": 1917.0, "bf16_tflops_sustained": 1700.0, "source": "measured"}
+    r = bench.tdvp_roofline(ks, pk, 3, ms)
+    assert r["kernel"] == "gemm" and r["bound"] == "tensor" and r["unit"] == "TFLOP/s"
+    assert r["dominant_class"] == "gemm"
+    assert abs(r["achieved"] - 16.92) < 1e-3
+    assert abs(r["frac"] - 16.92 / 1917.0) < 1e-5
+    assert abs(r["peak_3xtf32_derived"] - 319.5) < 0.1
+    assert abs(r["frac_of_3xtf32"] - 16.92 / 319.5) < 1e-3
+    assert abs(r["step_algorithmic_tflops"] - (16.92 * 4.373 + 0.653 * 3.387) / (ms / 1e3)) < 1e-3
+    assert abs(sum(r["kernel_time_share"].values()) - 1.0) < 1e-3
+    json.dumps(r)
+    # no kernel time recorded: no division by zero
+    empty = {k: {"launches": 0.0, "ms": 0.0, "flops": 0.0, "bytes": 0.0} for k in bench.KCLASS}
+    json.dumps(bench.tdvp_roofline(empty, pk, 1, 0.0))
