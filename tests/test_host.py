@@ -194,3 +194,32 @@ def test_bench_roofline_arithmetic():
     # no kernel time recorded: no division by zero
     empty = {k: {"launches": 0.0, "ms": 0.0, "flops": 0.0, "bytes": 0.0} for k in bench.KCLASS}
     json.dumps(bench.tdvp_roofline(empty, pk, 1, 0.0))
+
+
+def test_chain_desc_packing_roundtrip():
+    """chain_desc packs the MPS and MPO tensors concatenated in C order (the layout
+    qca_chain_desc documents) with their bond arrays; unpack_mps inverts it."""
+    from qca_gb300.algorithms import chain_desc, unpack_mps
+    rng = np.random.default_rng(3)
+    n = 5
+    D = [1, 2, 4, 3, 2, 1]
+    A = [rng.standard_normal((2, D[i], D[i + 1])) + 1j * rng.standard_normal((2, D[i], D[i + 1])) for i in range(n)]
+    W = MPO.hamiltonian_from_rules(Rules(n, range(1, 2), 1)).W
+    d, keep = chain_desc(A, W, "2tdvp", 0.05, 16, 1e-10)
+    mps_bonds, mpo_bonds, mps, mpo = keep
+    assert list(mps_bonds) == D
+    assert list(mpo_bonds) == [W[0].shape[2]] + [w.shape[3] for w in W]
+    assert d.n_sites == n and d.algorithm == _lib.QCA_ALGO_2TDVP and d.max_bond_dim == 16
+    flat = mps.view(np.complex128)
+    assert flat.size == sum(a.size for a in A)
+    back = unpack_mps(flat, D)
+    assert all(np.array_equal(x, y) for x, y in zip(back, A))
+    # the MPO block of site i starts after the blocks of sites < i, C order
+    off = 0
+    for w in W:
+        assert np.array_equal(mpo.view(np.complex128)[off:off + w.size].reshape(w.shape), w)
+        off += w.size
+    with pytest.raises(ValueError):
+        chain_desc(A, W[:-1], "2tdvp", 0.05, 16, 1e-10)
+    with pytest.raises(ValueError):
+        chain_desc(A, W, "exact", 0.05, 16, 1e-10)
