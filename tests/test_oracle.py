@@ -1,5 +1,8 @@
 """The oracle against the reference's own outputs (golden fixtures made by
-tests/golden/make_golden.py from the reference implementation)."""
+tests/golden/make_golden.py from the reference implementation), and against
+properties of the dynamics that hold at any size: a real symmetric Hamiltonian,
+unitary and time-reversible exact evolution, and 2TDVP at full bond dimension
+tracking the exact evolution with its integrator's order."""
 import numpy as np
 import pytest
 
@@ -87,3 +90,43 @@ def test_truncation_rule():
     assert O.truncation_rank(s, 10, 1e-8) == 3
     assert O.truncation_rank(s, 2, 1e-8) == 2
     assert O.truncation_rank(s, 10, 1e-13) == 5
+
+
+@pytest.mark.parametrize("d,lo,hi", RULES)
+def test_oracle_hamiltonian_is_real_symmetric(d, lo, hi):
+    """H = sum_i X_i P_i(neighbours) is a real symmetric 0/1 matrix for every rule."""
+    H = O.sparse_rule_hamiltonian(7, d, range(lo, hi))
+    assert abs(H - H.T).max() == 0
+    assert np.all(np.isin(H.data, [0.0, 1.0]))
+
+
+def test_oracle_exact_is_unitary_and_reversible():
+    n, d, rule = 8, 2, range(2, 4)
+    psi0 = O.product_state_vector(np.sin(O.random_thetas(n, 5)) ** 2)
+    psi = O.exact_evolve(psi0, n, d, rule, 0.07, 3)
+    assert abs(np.linalg.norm(psi) - 1.0) < 1e-12
+    back = O.exact_evolve(psi, n, d, rule, -0.07, 3)
+    assert np.abs(back - psi0).max() < 1e-10
+
+
+def test_oracle_2tdvp_full_bond_tracks_exact():
+    """At full bond dimension the gauge-consistent 2TDVP differs from the exact
+    evolution only by its integrator error, which falls by about 2^3 when dt halves
+    (distance 1, interval [1,1], centre cell alive, N = 6)."""
+    n, d, lo, hi = 6, 1, 1, 2
+    p = np.zeros(n)
+    p[n // 2] = 1.0
+    W = O.build_mpo(O.Rules(n, range(lo, hi), d))
+    worst = {}
+    for dt, steps in [(0.1, 5), (0.05, 10)]:
+        orc = O.TDVPOracle(O.mps_from_density_distribution(p), W, "2tdvp", dt, 64, 1e-14, fixed=True)
+        psi = O.product_state_vector(p)
+        w = 0.0
+        for _ in range(steps):
+            orc.step()
+            psi = O.exact_evolve(psi, n, d, range(lo, hi), dt, 1)
+            w = max(w, np.abs(O.populations_from_vector(O.mps_as_vector(orc.A), n)
+                              - O.populations_from_vector(psi, n)).max())
+        worst[dt] = w
+    assert worst[0.1] < 5e-5 and worst[0.05] < 5e-6
+    assert worst[0.1] / worst[0.05] > 4.0
