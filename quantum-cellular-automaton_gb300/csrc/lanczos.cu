@@ -5,9 +5,11 @@
 // the assembled effective Hamiltonian (lautils.py:44-81, tdvp.py:349-365,
 // tdvp.py:164-188).  Here v <- exp(-i tau H_eff) v is computed by Lanczos with
 // the basis resident on the device and classical Gram-Schmidt applied twice
-// (projections accumulated in FP64); after every iteration one warp per problem
-// evaluates exp(-i tau T) e_1 of the tridiagonal T by a sub-stepped Taylor
-// series (FP64) and stops when beta_j |(exp(-i tau T) e_1)_j| < tol.
+// (projections accumulated in FP64).  At the convergence check points (every
+// third iteration, on breakdown and at the iteration limit) one warp per problem
+// evaluates exp(-i tau T) e_1 of the tridiagonal T by a sub-stepped Taylor series
+// (FP64) and stops when beta_j |(exp(-i tau T) e_1)_j| < tol; in between it only
+// records beta_j.  A finished problem's later launches return at once (done flag).
 #include "tdvp_kernels.cuh"
 
 namespace qca {
