@@ -8,7 +8,9 @@
 // that update is one grouped launch over all chains (tdvp_kernels.cuh).  The
 // host mirrors the bond dimensions; it synchronises once per tick to learn the
 // truncated bond dimensions of the 2-site splits, and every few Lanczos
-// iterations to stop when every local exponential has converged.
+// iterations to stop when every local exponential has converged.  Chains added
+// since the last operation are initialised (TDVP.__init__) together, one grouped
+// launch per sweep position, before the next step or measurement.
 //
 // Gauge handling (what "parity" means for TDVP):
 //  * 2TDVP is evolved in the gauge-consistent form: the environments always
