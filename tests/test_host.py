@@ -7,7 +7,6 @@ import re
 import numpy as np
 import pytest
 
-import qca_gb300
 from qca_gb300 import _lib
 from qca_gb300.tensor_networks import MPO, MPS, Rules, rule_from_mpo
 
