@@ -10,7 +10,10 @@ the device.  <n_i> is streamed back every ``stream_every`` steps and at the end
 of each job through ``on_populations(job_id, step, populations)``.  A round steps
 the resident jobs in groups of at most ``group`` (one engine call each); with a
 deadline, the groups left when it passes wait for the next round, so a bounded
-run overruns its wall time by at most one group step.
+run overruns its wall time by at most one group step.  The callbacks run on a
+completion thread (the submission thread drives the engine alone), so user code
+that consumes the streamed populations overlaps with the next round on the GPU;
+``close()`` (called at the end of ``run``) drains it.
 
 This replaces the reference's per-state driver loop (``quantum_game.py:28-119``:
 one initial state at a time, measure every plot interval) with a multi-job
@@ -19,6 +22,8 @@ server; the per-job arithmetic is the same as a job run alone.
 from __future__ import annotations
 
 import ctypes
+import queue
+import threading
 import time
 from collections import deque
 from dataclasses import dataclass, field
@@ -54,6 +59,9 @@ class Server:
         self.max_resident = max_resident
         self.group = group if group is not None else max_resident
         self.on_populations = on_populations
+        self._done_q: queue.Queue | None = None
+        self._done_thread: threading.Thread | None = None
+        self.callback_errors: list[BaseException] = []
         self.pending: deque[JobState] = deque()
         self.active: list[JobState] = []
         self.done: list[JobState] = []
@@ -109,7 +117,7 @@ class Server:
             o += j.spec.n
             j.stream.append((j.steps_done, p))
             if self.on_populations:
-                self.on_populations(j.job_id, j.steps_done, p)
+                self._deliver(j.job_id, j.steps_done, p)
 
     # ------------------------------------------------------------------ loop
     def round(self, now: float | None = None, deadline: float | None = None) -> bool:
@@ -151,6 +159,33 @@ class Server:
         self.active = still
         return True
 
+    # ------------------------------------------------------------------ completion thread
+    def _deliver(self, job_id: int, step: int, populations: np.ndarray) -> None:
+        if self._done_thread is None:
+            self._done_q = queue.Queue()
+            self._done_thread = threading.Thread(target=self._completions, name="qca-serving-completions",
+                                                 daemon=True)
+            self._done_thread.start()
+        self._done_q.put((job_id, step, populations))
+
+    def _completions(self) -> None:
+        while True:
+            item = self._done_q.get()
+            if item is None:
+                return
+            try:
+                self.on_populations(*item)
+            except BaseException as e:  # kept for the caller; the loop keeps serving
+                self.callback_errors.append(e)
+
+    def close(self) -> None:
+        """Wait until every streamed population has been handed to the callback."""
+        if self._done_thread is not None:
+            self._done_q.put(None)
+            self._done_thread.join()
+            self._done_thread = None
+            self._done_q = None
+
     def run(self, jobs: list[Job], time_limit: float | None = None) -> dict:
         """Replay a request trace in real time (arrival offsets in seconds)."""
         t0 = time.perf_counter()
@@ -166,6 +201,7 @@ class Server:
             self.round(now if time_limit is None or now - t0 < time_limit else t0,
                        None if time_limit is None else t0 + time_limit)
         elapsed = time.perf_counter() - t0
+        self.close()
         return self.report(elapsed)
 
     def report(self, elapsed: float) -> dict:

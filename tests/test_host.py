@@ -123,12 +123,10 @@ def test_poisson_trace_shape():
     assert all(50 <= j.spec.steps <= 500 for j in jobs)
 
 
-def test_serving_round_stops_at_its_deadline(monkeypatch):
-    """The serving loop's host logic with the engine faked: a round steps the
-    resident jobs group by group and leaves the groups after its deadline for the
-    next round; a bounded run overruns its wall time by at most one group step."""
+def _fake_serving(monkeypatch):
+    """The serving module with its engine faked on the host: every engine call of a
+    step takes one second of a fake clock."""
     from qca_gb300 import serving
-    from qca_gb300.workloads import ChainSpec
     clock = {"t": 0.0}
     stepped = []
 
@@ -150,6 +148,15 @@ def test_serving_round_stops_at_its_deadline(monkeypatch):
     monkeypatch.setattr(serving._lib, "call", fake_call)
     monkeypatch.setattr(serving.time, "perf_counter", lambda: clock["t"])
     monkeypatch.setattr(serving.time, "sleep", lambda s: clock.__setitem__("t", clock["t"] + s))
+    return serving, clock, stepped
+
+
+def test_serving_round_stops_at_its_deadline(monkeypatch):
+    """The serving loop's host logic with the engine faked: a round steps the
+    resident jobs group by group and leaves the groups after its deadline for the
+    next round; a bounded run overruns its wall time by at most one group step."""
+    from qca_gb300.workloads import ChainSpec
+    serving, clock, stepped = _fake_serving(monkeypatch)
     spec = ChainSpec(n=6, distance=1, interval=range(1, 2), chi=4, p=np.full(6, 0.5), steps=100)
     srv = serving.Server("mixed", hbm_budget_bytes=1 << 30, stream_every=1000, max_resident=5, group=2)
     for _ in range(5):
@@ -222,3 +229,31 @@ def test_chain_desc_packing_roundtrip():
         chain_desc(A, W[:-1], "2tdvp", 0.05, 16, 1e-10)
     with pytest.raises(ValueError):
         chain_desc(A, W, "exact", 0.05, 16, 1e-10)
+
+
+def test_serving_callbacks_run_on_a_completion_thread(monkeypatch):
+    """Streamed populations reach the callback on the completion thread, in the
+    order they were measured, all of them by the time run() returns; a callback
+    that raises is recorded and the loop keeps serving."""
+    import threading
+    from qca_gb300.workloads import ChainSpec
+    serving, clock, stepped = _fake_serving(monkeypatch)
+    seen, threads = [], set()
+
+    def on_pop(job_id, step, pop):
+        threads.add(threading.get_ident())
+        seen.append((job_id, step, pop.shape))
+        if job_id == 1 and step == 2:
+            raise RuntimeError("consumer failed")
+
+    srv = serving.Server("mixed", hbm_budget_bytes=1 << 30, stream_every=1, max_resident=4,
+                         on_populations=on_pop)
+    spec = ChainSpec(n=5, distance=1, interval=range(1, 2), chi=4, p=np.full(5, 0.5), steps=3)
+    for _ in range(2):
+        srv.submit(spec, arrival=0.0)
+    rep = srv.run([], time_limit=None)
+    assert rep["jobs_done"] == 2
+    assert seen == [(0, 1, (5,)), (1, 1, (5,)), (0, 2, (5,)), (1, 2, (5,)), (0, 3, (5,)), (1, 3, (5,))]
+    assert threading.get_ident() not in threads and len(threads) == 1
+    assert len(srv.callback_errors) == 1
+
