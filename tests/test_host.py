@@ -257,3 +257,23 @@ def test_serving_callbacks_run_on_a_completion_thread(monkeypatch):
     assert threading.get_ident() not in threads and len(threads) == 1
     assert len(srv.callback_errors) == 1
 
+
+
+def test_batched_workload_definition():
+    """The benchmark's batched workload: 256 chains drawn from one seed with
+    N ~ U{16..96}, distance in {1,2,3}, interval in {[1,1],[2,3],[2,4]}, bond cap in
+    {32,64,128}, random product states, dt = 0.05; the same seed gives the same
+    chains, each rank's seed its own."""
+    from qca_gb300 import workloads as W
+    a, b, c = W.chain_mix(256, seed=1000), W.chain_mix(256, seed=1000), W.chain_mix(256, seed=1001)
+    assert len(a) == 256
+    assert all(16 <= s.n <= 96 for s in a)
+    assert {s.distance for s in a} == {1, 2, 3}
+    assert {(s.interval.start, s.interval.stop) for s in a} == {(1, 2), (2, 4), (2, 5)}
+    assert {s.chi for s in a} == {32, 64, 128}
+    assert all(s.dt == 0.05 and s.algorithm == "2tdvp" and s.p.shape == (s.n,) for s in a)
+    assert all(np.all((s.p >= 0) & (s.p <= 1)) for s in a)
+    assert [(s.n, s.chi, s.distance) for s in a] == [(s.n, s.chi, s.distance) for s in b]
+    assert all(np.array_equal(x.p, y.p) for x, y in zip(a, b))
+    assert [(s.n, s.chi) for s in a] != [(s.n, s.chi) for s in c]
+    assert sum(s.site_updates_per_step() for s in a) == sum(2 * (s.n - 1) for s in a)
