@@ -43,7 +43,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batched", choices=["batched", "exact", "single", "accuracy", "serving"])
-    ap.add_argument("--serve-seconds", type=float, default=60.0)
+    ap.add_argument("--serve-seconds", type=float, default=120.0)
+    ap.add_argument("--serve-jobs", type=int, default=64)
+    ap.add_argument("--serve-step-scale", type=int, default=10)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--chains", type=int, default=256)
     ap.add_argument("--no-e2e", action="store_true")
@@ -229,35 +231,97 @@ def get_mps(eng, cid, n):
     return unpack_mps(flat, [int(x) for x in b])
 
 
-def cpu_tdvp_sample(specs, budget_s: float):
-    """Time the reference algorithm (the oracle's restatement of tdvp.py: dense
-    effective Hamiltonian + eigh per local update, the reference's cost profile)
-    on the host cores: chain 0 of the same workload, evolved from its product
-    state one local update at a time until the time budget is used; returns
-    (site-updates/s, description).  The dense local problems grow as
-    (4 chi^2)^3, so the sample covers the first updates only."""
-    from oracle import qca_oracle as O
-    spec = specs[0]
-    W = O.build_mpo(O.Rules(spec.n, spec.interval, spec.distance))
-    orc = O.TDVPOracle(O.mps_from_density_distribution(spec.p), W, spec.algorithm, spec.dt, spec.chi, spec.eps)
-    done, t_used, steps = 0, 0.0, 0
-    while t_used < budget_s and steps < 50:
-        it = orc.step_updates()
-        while t_used < budget_s:
+class RefSampler:
+    """Bounded timing of the reference algorithm on the host cores: the oracle's
+    restatement of tdvp.py (dense effective Hamiltonian + eigh per local update,
+    the reference's own cost profile) evolving the chains of the workload in order
+    from their product states.  ``sample(budget)`` runs local updates until the
+    budget is used and never starts one whose predicted time (a + c n^3 for the
+    local dimension n, calibrated on the updates run so far and on one eigh timed
+    at start) exceeds what is left; a chain whose next update would not fit even a
+    whole budget is retired and the next chain of the workload begins.  The
+    sample therefore covers the cheap early updates of each chain, which makes the
+    host rate an overestimate of the reference at the device run's bond
+    dimensions."""
+
+    def __init__(self, specs, per_update_limit_s: float):
+        from oracle import qca_oracle as O
+        self.O = O
+        self.specs = specs
+        self.limit = per_update_limit_s
+        self.ci = -1
+        self.done = 0
+        self.used = 0.0
+        self.retired = []
+        self.max_bond = 0
+        self.max_n = 0
+        m = np.random.default_rng(0).standard_normal((768, 768))
+        h = m + m.T
+        t0 = time.perf_counter()
+        np.linalg.eigh(h.astype(np.complex128))
+        self.c = (time.perf_counter() - t0) / 768.0 ** 3
+        self.a = 0.0
+        self._next_chain()
+
+    def _next_chain(self):
+        self.ci += 1
+        spec = self.specs[self.ci % len(self.specs)]
+        W = self.O.build_mpo(self.O.Rules(spec.n, spec.interval, spec.distance))
+        self.orc = self.O.TDVPOracle(self.O.mps_from_density_distribution(spec.p), W, spec.algorithm, spec.dt,
+                                     spec.chi, spec.eps)
+        self.it = self.orc.step_updates()
+
+    def predict(self, n: int) -> float:
+        return self.a + 1.2 * self.c * float(n) ** 3
+
+    def sample(self, budget: float):
+        done, used = 0, 0.0
+        while used < budget:
+            n = self.orc.upcoming_size()
+            if self.predict(n) > self.limit:
+                self.retired.append((self.ci, self.specs[self.ci % len(self.specs)].n, n))
+                self._next_chain()
+                continue
+            if used + self.predict(n) > budget:
+                break
             t0 = time.perf_counter()
             try:
-                next(it)
+                next(self.it)
+                ok = True
             except StopIteration:
-                t_used += time.perf_counter() - t0
-                break
-            t_used += time.perf_counter() - t0
-            done += 1
-        steps += 1
-    chi = max(a.shape[2] for a in orc.A)
-    return done / t_used, (
-        f"chain 0 of the workload (N={spec.n}, d={spec.distance}, interval {spec.interval}, cap {spec.chi}): "
-        f"{done} reference local updates from the product state (bonds reached {chi}), "
-        f"{int(os.environ.get('OMP_NUM_THREADS', os.cpu_count()))} BLAS threads")
+                self.it = self.orc.step_updates()
+                ok = False
+            dt = time.perf_counter() - t0
+            used += dt
+            if ok:
+                done += 1
+                self.max_n = max(self.max_n, n)
+                self.max_bond = max(self.max_bond, max(a.shape[2] for a in self.orc.A))
+                if n <= 64:
+                    self.a = dt if self.a == 0.0 else min(self.a, dt)
+                elif n >= 512:
+                    self.c = max(self.c, (dt - self.a) / float(n) ** 3)
+        self.done += done
+        self.used += used
+        return done, used
+
+    def rate(self) -> float:
+        return self.done / self.used if self.used > 0 else 0.0
+
+    def describe(self) -> str:
+        return (f"{self.done} local updates of the reference algorithm (oracle restatement of tdvp.py: dense "
+                f"effective Hamiltonian + eigh) in {self.used:.1f} s, evolving chains 0..{self.ci} of the workload "
+                f"from their product states; bonds reached {self.max_bond}, largest local problem {self.max_n}; "
+                f"{len(self.retired)} chain(s) retired when their next update was predicted to exceed "
+                f"{self.limit:.0f} s; {int(os.environ.get('OMP_NUM_THREADS', os.cpu_count()))} BLAS threads")
+
+
+def cpu_tdvp_sample(specs, budget_s: float):
+    """(site-updates/s, description) of the reference algorithm on the host cores
+    over a bounded sample of the workload (``RefSampler``)."""
+    rs = RefSampler(specs, per_update_limit_s=min(5.0, budget_s / 3))
+    rs.sample(budget_s)
+    return rs.rate(), rs.describe()
 
 
 def run_tdvp(args, dist: Dist):
@@ -449,44 +513,24 @@ def run_reference(args, dist: Dist):
                 "e2e": {"value": round(v, 1), "unit": "amplitude-updates/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
     specs, desc = build_specs(args, 0)
-    # each step is a bounded sample of the workload: local updates of chain 0 of
-    # the mix with the reference algorithm, continuing from where the previous
-    # sample stopped, for at most 20 s of host time
-    spec = specs[0]
-    W_ = O.build_mpo(O.Rules(spec.n, spec.interval, spec.distance))
-    orc = O.TDVPOracle(O.mps_from_density_distribution(spec.p), W_, spec.algorithm, spec.dt, spec.chi, spec.eps)
-    it = orc.step_updates()
-
-    def sample(budget):
-        nonlocal it
-        done, used = 0, 0.0
-        while used < budget:
-            t0 = time.perf_counter()
-            try:
-                next(it)
-                done += 1
-            except StopIteration:
-                it = orc.step_updates()
-            used += time.perf_counter() - t0
-        return done, used
-
+    # each step is a bounded sample of the workload (RefSampler): local updates of
+    # the reference algorithm on the chains of the mix, at most 6 s per step
+    rs = RefSampler(specs, per_update_limit_s=4.0)
     for _ in range(args.warmup):
-        sample(2.0)
-    tot_done, tot_used = 0, 0.0
+        rs.sample(1.0)
+    rs.done, rs.used = 0, 0.0
+    per_step = []
     for _ in range(args.steps):
-        d_, u_ = sample(20.0)
-        tot_done += d_
-        tot_used += u_
-    v = tot_done / tot_used
-    chi = max(a.shape[2] for a in orc.A)
+        d_, u_ = rs.sample(6.0)
+        per_step.append(u_)
+    v = rs.rate()
     return {"impl": "reference", "metric": "site-updates/s", "value": round(v, 3), "unit": "site-updates/s",
             "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": round(tot_used / args.steps * 1e3, 2), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": {"workload": desc},
+            "ms_per_step": round(rs.used / max(1, args.steps) * 1e3, 2), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": desc},
             "cpu_baseline": {"value": round(v, 3), "unit": "site-updates/s", "cores": os.cpu_count(), "kind": "port",
-                             "sample": f"chain 0 of the mix (N={spec.n}, d={spec.distance}, cap {spec.chi}): "
-                                       f"{tot_done} local updates of the oracle restatement of tdvp.py from the "
-                                       f"product state (20 s per step, bonds reached {chi})"},
+                             "sample": rs.describe()},
             "e2e": {"value": round(v, 3), "unit": "site-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -544,31 +588,65 @@ def run_accuracy(args, dist: Dist):
             "mixed_over_fp64_speedup": round(rates["mixed"] / rates["fp64"], 2)}
 
 
-def run_serving(args, dist: Dist):
-    """The serving configuration replayed in real time for a bounded wall time:
-    Poisson(200/s) arrivals of 1TDVP/2TDVP jobs, N ~ U{12..128}, distance in
-    {1,2}, bond cap in {16,...,256}, 50-500 steps, dt = 0.05, 150 GB budget,
-    <n_i> streamed every 10 steps.  Reports completed jobs, p50/p99 latency,
-    site-updates/s, and the backlog left when the wall time ran out."""
-    import torch
+def serving_trace(args, rank: int):
+    """A bounded slice of the serving configuration: the first ``--serve-jobs``
+    requests of the Poisson(200/s) trace (1TDVP/2TDVP, N ~ U{12..128}, distance in
+    {1,2}, bond cap in {16,...,256}, dt = 0.05) with their step counts (50-500)
+    divided by ``--serve-step-scale`` so that the slice runs to completion."""
     from qca_gb300 import workloads as W
+    jobs = W.poisson_jobs(rate=200.0, duration=60.0, seed=7 + rank)[:args.serve_jobs]
+    for j in jobs:
+        j.spec.steps = max(1, -(-j.spec.steps // args.serve_step_scale))
+    return jobs
+
+
+def run_serving(args, dist: Dist):
+    """The serving loop on a bounded slice of the serving configuration, replayed
+    in real time (arrivals at their trace offsets), once with the mixed path and
+    once with the plain FP64 path on the same requests, each until every job is
+    done or ``--serve-seconds`` have passed.  Reports completed jobs, p50/p99
+    latency (arrival to last populations), site-updates/s of both paths and their
+    ratio, and max|d<n_i>| between the two paths' streamed populations of the jobs
+    both completed."""
+    import torch
     from qca_gb300.serving import Server
     torch.cuda.set_device(dist.local)
-    jobs = W.poisson_jobs(rate=200.0, duration=60.0, seed=7 + dist.rank)
-    srv = Server(args.precision, hbm_budget_bytes=150 << 30, stream_every=10, max_resident=args.chains, group=16)
-    rep = srv.run(jobs, time_limit=args.serve_seconds)
-    return {"metric": "site-updates/s", "value": round(rep["site_updates_per_s"], 1), "unit": "site-updates/s",
-            "n_gpus": dist.world, "higher_is_better": True, "data": "synthetic",
-            "config": {"workload": "serving: Poisson 200/s over 60 s, 1TDVP/2TDVP, N~U{12..128}, d in {1,2}, "
-                                   "chi in {16..256}, 50-500 steps, dt=0.05, HBM budget 150 GB",
-                       "wall_limit_s": args.serve_seconds, "precision": args.precision,
-                       "max_resident_jobs": args.chains, "jobs_per_engine_call": 16,
-                       "jobs_in_trace": len(jobs)},
-            "p50_latency_s": rep["p50_latency_s"], "p99_latency_s": rep["p99_latency_s"],
-            "p50_step_round_s": rep["p50_round_s"], "p99_step_round_s": rep["p99_round_s"],
-            "p50_first_populations_s": rep["p50_first_stream_s"], "p99_first_populations_s": rep["p99_first_stream_s"],
-            "jobs_done": rep["jobs_done"], "jobs_active": rep["jobs_active"], "jobs_pending": rep["jobs_pending"],
-            "elapsed_s": round(rep["elapsed_s"], 1)}
+    reps, streams = {}, {}
+    for prec in ("mixed", "fp64"):
+        jobs = serving_trace(args, dist.rank)
+        srv = Server(prec, hbm_budget_bytes=150 << 30, stream_every=10, max_resident=args.chains,
+                     ticks_per_round=32)
+        reps[prec] = srv.run(jobs, time_limit=args.serve_seconds)
+        streams[prec] = {j.job_id: j.stream for j in srv.done}
+        del srv
+    both = set(streams["mixed"]) & set(streams["fp64"])
+    dn = 0.0
+    for k in both:
+        for (sa, pa), (sb, pb) in zip(streams["mixed"][k], streams["fp64"][k]):
+            dn = max(dn, float(np.abs(pa - pb).max()))
+    jobs = serving_trace(args, dist.rank)
+    m, f = reps["mixed"], reps["fp64"]
+
+    def summary(r):
+        return {"site_updates_per_s": round(r["site_updates_per_s"], 1), "jobs_done": r["jobs_done"],
+                "jobs_failed": r["jobs_failed"], "jobs_unfinished": r["jobs_active"] + r["jobs_pending"],
+                "p50_latency_s": r["p50_latency_s"], "p99_latency_s": r["p99_latency_s"],
+                "p50_first_populations_s": r["p50_first_stream_s"],
+                "p99_first_populations_s": r["p99_first_stream_s"], "max_resident_jobs": r["max_resident"],
+                "p50_round_s": r["p50_round_s"], "elapsed_s": round(r["elapsed_s"], 1)}
+
+    return {"metric": "site-updates/s", "value": round(m["site_updates_per_s"], 1), "unit": "site-updates/s",
+            "n_gpus": dist.world, "higher_is_better": True, "data": "synthetic", "dtype": "f32+f64",
+            "config": {"workload": f"serving: the first {len(jobs)} requests of the Poisson(200/s) trace "
+                                   "(1TDVP/2TDVP, N~U{12..128}, d in {1,2}, chi in {16..256}, dt=0.05), step counts "
+                                   f"50-500 divided by {args.serve_step_scale}, replayed in real time, HBM budget "
+                                   "150 GB, <n_i> streamed every 10 steps",
+                       "wall_limit_s_per_path": args.serve_seconds, "ticks_per_round": 32},
+            "p50_latency_s": m["p50_latency_s"], "p99_latency_s": m["p99_latency_s"],
+            "mixed": summary(m), "fp64": summary(f),
+            "mixed_over_fp64": round(m["site_updates_per_s"] / f["site_updates_per_s"], 2)
+            if f["site_updates_per_s"] > 0 else None,
+            "accuracy": {"max_dn_vs_fp64": dn, "jobs_compared": len(both)}}
 
 
 def main():

@@ -136,10 +136,28 @@ int qca_chain_footprint(const qca_chain_desc* d, int precision, size_t* bytes);
  * Returns QCA_ERR_ADMISSION when the budget would be exceeded. */
 int qca_chain_add(qca_engine* e, const qca_chain_desc* d, void* stream, int* chain_id);
 int qca_chain_remove(qca_engine* e, int chain_id);
-/* TDVP.do_time_step (tdvp.py:50-63) nsteps times for every chain of the engine. */
+/* TDVP.do_time_step (tdvp.py:50-63) nsteps times for every chain of the engine.
+ * A chain that fails numerically does not stop the others: they complete their
+ * steps and the call returns the failure (QCA_ERR_NAN before
+ * QCA_ERR_NOT_CONVERGED) naming the first failed chain. */
 int qca_engine_step(qca_engine* e, int nsteps, void* stream);
 /* do_time_step nsteps times for the listed chains only (the others keep their state). */
 int qca_engine_step_chains(qca_engine* e, const int* chain_ids, int count, int nsteps, void* stream);
+/* Continuous batching (no counterpart in the reference, which evolves one state at
+ * a time): qca_chain_schedule adds nsteps time steps to a chain's budget, and
+ * qca_engine_advance runs at most max_ticks lock-step ticks over the listed chains
+ * (all chains when count = 0), one local update of every chain inside a time step
+ * per tick; a chain that completes a step begins its next scheduled one at the
+ * following tick, so chains of different length and bond dimension progress
+ * independently and new chains join at any tick.  A call may stop inside a time
+ * step; measurements and qca_chain_get_mps need the chain at a step boundary.
+ * Chains that fail (QCA_ERR_NAN / QCA_ERR_NOT_CONVERGED, named in the message) are
+ * skipped by later calls and stay failed until removed.  qca_chain_progress
+ * writes 4 values: [0] time steps completed since the chain was added, [1] steps
+ * scheduled and not completed, [2] 1 while inside a step, [3] failure status. */
+int qca_chain_schedule(qca_engine* e, int chain_id, int nsteps);
+int qca_engine_advance(qca_engine* e, const int* chain_ids, int count, int max_ticks, void* stream);
+int qca_chain_progress(qca_engine* e, int chain_id, long long* progress);
 /* Algorithm.measure (algorithm.py:58-63 -> mps.py:100-140).  1TDVP chains: mutates
  * the gauge of the stored MPS exactly like the reference.  2TDVP chains whose
  * orthogonality centre is at site 0 (the state after every step): the same left QR
@@ -161,6 +179,12 @@ int qca_chain_get_mps(qca_engine* e, int chain_id, double* mps, size_t capacity,
 /* Statistics of the last step of a chain: [0] largest Lanczos dimension used,
  * [1] summed discarded weight (sum of squared truncated singular values). */
 int qca_chain_stats(qca_engine* e, int chain_id, double* stats);
+/* The first `count` (at most 5) statistics of a chain: [0] and [1] as
+ * qca_chain_stats, [2] the most Jacobi sweeps one two-site split of the last step
+ * needed, [3] the chain's failure status (0, or the QCA_ERR_* code of the step in
+ * which it failed), [4] the device bytes the chain holds.  No counterpart in the
+ * reference (whose LAPACK calls report nothing of the kind). */
+int qca_chain_stats_ex(qca_engine* e, int chain_id, double* stats, int count);
 
 /* Profiling hook (no counterpart in the reference, which has no tracing): when
  * enabled, every grouped launch is bracketed by CUDA events on its stream.
@@ -183,6 +207,13 @@ int qca_test_gemm_c64(int M, int N, int K, const void* A, const void* B, void* C
  * output arrays need room for k = min(2 Dl, 2 Dr).  Synchronises the stream. */
 int qca_test_svd(int precision, int Dl, int Dr, const void* theta, int chi, double eps, void* Al, void* Ar,
                  double* sv, int* k_out, void* stream);
+/* Test hook (no counterpart in the reference): qca_test_svd with the Jacobi sweep
+ * limit lowered to max_sweeps (0 = the default of 24), so that the
+ * QCA_ERR_NOT_CONVERGED path can be exercised on a well-posed problem.  Returns
+ * QCA_ERR_NOT_CONVERGED when the sweeps ran out and QCA_ERR_NAN for non-finite
+ * input; the outputs are written in either case. */
+int qca_test_svd_sweeps(int precision, int Dl, int Dr, const void* theta, int chi, double eps, int max_sweeps,
+                        void* Al, void* Ar, double* sv, int* k_out, void* stream);
 
 #ifdef __cplusplus
 }

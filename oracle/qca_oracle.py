@@ -396,6 +396,7 @@ class TDVPOracle:
         for site in reversed(range(1, n)):
             make_site_canonical(self.A, site - 1)
             self._update_env("right", site)
+        self._upcoming = self._pair_size(0) if algorithm == "2tdvp" else self._site_size(0)
 
     # environments -----------------------------------------------------------------
     def _env(self, side: str, site: int) -> np.ndarray:
@@ -417,22 +418,25 @@ class TDVPOracle:
             self._update_env("right", site)
 
     # local evolutions -------------------------------------------------------------
+    def _local_exp(self, L: np.ndarray, R: np.ndarray, W, v: np.ndarray, step: float) -> np.ndarray:
+        """exp(-i pi/2 step H_eff) applied like ``lautils.timestep``: the dense
+        effective Hamiltonian of ``tdvp.py:298-326`` (``W is None``: the bond
+        matrix K_eff) and its full eigendecomposition, the reference's own method."""
+        h = _keff_bond(L, R) if W is None else _heff_site(L, R, W)
+        return _local_step(h, v.reshape(-1), step).reshape(v.shape)
+
     def _evolve_site(self, site: int, step: float) -> np.ndarray:
-        A = self.A[site]
-        h = _heff_site(self._env("left", site - 1), self._env("right", site + 1), self.W[site])
-        return _local_step(h, A.reshape(-1), step).reshape(A.shape)
+        return self._local_exp(self._env("left", site - 1), self._env("right", site + 1), self.W[site],
+                               self.A[site], step)
 
     def _evolve_bond(self, bond: int, C: np.ndarray) -> np.ndarray:
-        k = _keff_bond(self._env("left", bond - 1), self._env("right", bond))
-        return _local_step(k, C.reshape(-1), -self.dt / 2).reshape(C.shape)
+        return self._local_exp(self._env("left", bond - 1), self._env("right", bond), None, C, -self.dt / 2)
 
     def _split(self, Al, Ar, L, R, Wl, Wr):
         """``tdvp.py:270-296``."""
         sl, sr = Al.shape, Ar.shape
         th = np.tensordot(Al, Ar, (2, 1)).transpose(0, 2, 1, 3).reshape(sl[0] * sr[0], sl[1], sr[2])
-        W = _merge_w(Wl, Wr)
-        h = _heff_site(L, R, W)
-        th = _local_step(h, th.reshape(-1), self.dt / 2).reshape(th.shape)
+        th = self._local_exp(L, R, _merge_w(Wl, Wr), th, self.dt / 2)
         th = th.reshape(sl[0], sr[0], sl[1], sr[2]).transpose(0, 2, 1, 3).reshape(sl[0] * sl[1], sr[0] * sr[2])
         u, s, vh = np.linalg.svd(th, full_matrices=False)
         k = truncation_rank(s, self.chi, self.eps)
@@ -447,9 +451,23 @@ class TDVPOracle:
         for _ in self.step_updates():
             pass
 
+    def upcoming_size(self) -> int:
+        """Dimension of the next local problem of ``step_updates`` (the dense
+        effective Hamiltonian is this size squared and its eigh costs the cube):
+        4 D_l D_r for a 2TDVP bond update, 2 D_l D_r for a 1TDVP site update.
+        Lets a timing harness skip an update it could not finish in its budget."""
+        return self._upcoming
+
+    def _pair_size(self, l: int) -> int:
+        return 4 * self.A[l].shape[1] * self.A[l + 1].shape[2]
+
+    def _site_size(self, s: int) -> int:
+        return 2 * self.target[s] * self.target[s + 1]
+
     def step_updates(self):
         """One time step as a generator that yields after every local update
-        (bond update for 2TDVP, site update for 1TDVP), for bounded timing."""
+        (bond update for 2TDVP, site update for 1TDVP), for bounded timing;
+        ``upcoming_size`` gives the size of the update the next ``next`` runs."""
         make_site_canonical(self.A, 0)
         if self.fixed:
             self._refresh_right()
@@ -470,6 +488,7 @@ class TDVPOracle:
             if site < n - 2:
                 self._update_env("left", site)
                 self.A[site + 1] = self._evolve_site(site + 1, -self.dt / 2)
+            self._upcoming = self._pair_size(site + 1) if site < n - 2 else self._pair_size(n - 2)
             yield
 
     def _sweep_left_2(self):
@@ -482,6 +501,7 @@ class TDVPOracle:
             if site > 1:
                 self._update_env("right", site)
                 self.A[site - 1] = self._evolve_site(site - 1, -self.dt / 2)
+            self._upcoming = self._pair_size(site - 2) if site > 1 else self._pair_size(0)
             yield
 
     def _sweep_right_1(self):
@@ -492,6 +512,7 @@ class TDVPOracle:
             new_a = self._evolve_site(site, self.dt / 2)
             if site == n - 1:
                 self.A[site] = new_a
+                self._upcoming = self._site_size(n - 1)
                 yield
                 continue
             q, c = left_qr(new_a, reduced=False)
@@ -500,6 +521,7 @@ class TDVPOracle:
             c = truncate_and_pad(c, (tshape[2], c.shape[1]))
             c = self._evolve_bond(site + 1, c)
             self.A[site + 1] = np.tensordot(c, self.A[site + 1], (1, 1)).transpose(1, 0, 2)
+            self._upcoming = self._site_size(site + 1)
             yield
 
     def _sweep_left_1(self):
@@ -510,6 +532,7 @@ class TDVPOracle:
             new_a = self._evolve_site(site, self.dt / 2)
             if site == 0:
                 self.A[site] = new_a
+                self._upcoming = self._site_size(0)
                 yield
                 continue
             q, c = right_qr(new_a, reduced=False)
@@ -518,10 +541,74 @@ class TDVPOracle:
             c = truncate_and_pad(c, (c.shape[0], tshape[1]))
             c = self._evolve_bond(site, c)
             self.A[site - 1] = np.tensordot(self.A[site - 1], c, (2, 0))
+            self._upcoming = self._site_size(site - 1)
             yield
 
     def measure(self):
         return measure(self.A)
+
+
+def heff_apply(L: np.ndarray, R: np.ndarray, W, x: np.ndarray) -> np.ndarray:
+    """The operator the reference exponentiates, applied matrix free.
+
+    ``lautils.timestep`` returns tensordot(v, U, (0, 0)) = U^T v with U built from
+    the assembled matrix M[(s,a,c),(s',b,e)] = sum W[s,s',l,r] L[a,l,b] R[c,r,e]
+    (``tdvp.py:298-310``; ``tdvp.py:312-326`` without W for the bond), so the
+    operator is M^T:  y[s',b,e] = sum W[s,s',l,r] L[a,l,b] R[c,r,e] x[s,a,c].
+    Environments are (ket, w, bra) as in ``tdvp.py:328-347``."""
+    if W is None:
+        t = np.tensordot(x, L, (0, 0))                  # [c, l, b]
+        return np.tensordot(t, R, ((0, 1), (0, 1)))    # [b, e]
+    t = np.tensordot(x, L, (1, 0))                      # [s, c, l, b]
+    t = np.tensordot(W, t, ((0, 2), (0, 2)))            # [s', r, c, b]
+    y = np.tensordot(t, R, ((1, 2), (1, 0)))            # [s', b, e]
+    return y
+
+
+def krylov_expm(apply, v: np.ndarray, tau: float, tol: float = 1e-14, mmax: int = 80) -> np.ndarray:
+    """exp(-i tau H) v for a Hermitian H given as ``apply`` by Lanczos with full
+    reorthogonalisation (complex128) and the small exponential from the
+    eigendecomposition of the tridiagonal matrix; stops when the error estimate
+    beta_m |(exp(-i tau T) e_1)_m| falls below tol.  Substitutes for the dense
+    eigh of ``lautils.py:44-54`` where that is out of reach."""
+    shape = v.shape
+    v0 = v.reshape(-1).astype(np.complex128)
+    nrm = np.linalg.norm(v0)
+    if nrm == 0.0:
+        return np.zeros(shape, dtype=np.complex128)
+    V = [v0 / nrm]
+    alpha: list[float] = []
+    beta: list[float] = []
+    c = np.ones(1, dtype=np.complex128)
+    for j in range(min(mmax, v0.size)):
+        w = apply(V[j].reshape(shape)).reshape(-1)
+        alpha.append(float(np.real(np.vdot(V[j], w))))
+        for _ in range(2):
+            for u in V:
+                w = w - np.vdot(u, w) * u
+        b = float(np.linalg.norm(w))
+        T = np.diag(alpha) + np.diag(beta, 1) + np.diag(beta, -1)
+        ev, evec = np.linalg.eigh(T)
+        c = evec @ (np.exp(-1j * tau * ev) * evec[0].conj())
+        if b * abs(c[-1]) < tol or b < 1e-300 or j + 1 == v0.size:
+            break
+        beta.append(b)
+        V.append(w / b)
+    out = np.zeros_like(v0)
+    for k in range(len(c)):
+        out += c[k] * V[k]
+    return (nrm * out).reshape(shape)
+
+
+class TDVPKrylovOracle(TDVPOracle):
+    """``TDVPOracle`` with the local exponentials computed matrix free by Lanczos
+    (``heff_apply`` + ``krylov_expm``) instead of the dense effective Hamiltonian
+    and its eigh: the same algorithm (sweeps, splits, truncation, QR moves) at
+    bond dimensions where the reference's dense n x n problems (n = 4 D_l D_r) are
+    out of reach.  Validated against ``TDVPOracle`` at small bonds."""
+
+    def _local_exp(self, L, R, W, v, step):
+        return krylov_expm(lambda x: heff_apply(L, R, W, x), v, (np.pi / 2) * step)
 
 
 def truncation_rank(s: np.ndarray, max_bond_dim: int, epsilon: float) -> int:

@@ -92,15 +92,20 @@ SIGNATURES = {
     "qca_chain_remove": [_P, _I],
     "qca_engine_step": [_P, _I, _P],
     "qca_engine_step_chains": [_P, _PI, _I, _I, _P],
+    "qca_chain_schedule": [_P, _I, _I],
+    "qca_engine_advance": [_P, _PI, _I, _I, _P],
+    "qca_chain_progress": [_P, _I, ctypes.POINTER(ctypes.c_longlong)],
     "qca_chain_measure": [_P, _I, _PD, _PD, _PD, _PD, _P],
     "qca_engine_measure": [_P, _PI, _I, _PD, _PD, _PD, _PD, _P],
     "qca_chain_bonds": [_P, _I, _PI],
     "qca_chain_get_mps": [_P, _I, _PD, _SZ, _P],
     "qca_chain_stats": [_P, _I, _PD],
+    "qca_chain_stats_ex": [_P, _I, _PD, _I],
     "qca_engine_profile": [_P, _I],
     "qca_engine_kernel_stats": [_P, _PD, _I],
     "qca_test_gemm_c64": [_I, _I, _I, _P, _P, _P, _I, _P],
     "qca_test_svd": [_I, _I, _I, _P, _I, _D, _P, _P, _P, _PI, _P],
+    "qca_test_svd_sweeps": [_I, _I, _I, _P, _I, _D, _I, _P, _P, _P, _PI, _P],
 }
 
 _lib = None

@@ -21,6 +21,7 @@
 //    growth uses the complement columns of the complete QR (tdvp.py:74, 95).
 #include <algorithm>
 #include <cmath>
+#include <limits>
 #include <map>
 #include <memory>
 #include <vector>
@@ -147,18 +148,23 @@ struct Chain {
   double* lzP = nullptr;
   double* sv = nullptr;
   double* dscal = nullptr;  // [0] discarded weight of the current step, [1..4] rho
-  int* iflags = nullptr;    // [0] k_out, [1] svd status, [2] lanczos done copy
+  int* iflags = nullptr;    // [0] k_out, [1] svd status, [2] svd sweeps, [3] Lanczos failure bits
   void* mem = nullptr;
   size_t bytes = 0;
   int max_chunks = 1;
   // sweep state
   int dir = 0;  // 0 right, 1 left
   int pos = 0;
-  long long todo = 0;
+  long long todo = 0;  // time steps scheduled and not yet completed (the current one included)
+  bool in_step = false;  // a time step has begun and its sweeps are not finished
+  long long steps_done = 0;  // time steps completed since the chain was added
   int center = 0;     // orthogonality centre (0 after a full step)
   int lz_used = 0;    // largest Krylov dimension in the current step
+  int svd_sweeps = 0; // most Jacobi sweeps of a two-site split in the current step
   double disc_host = 0.0;
-  int status = 0;
+  int status = 0;             // QCA_ERR_NAN / QCA_ERR_NOT_CONVERGED once the chain has failed
+  int fail_site = -1;         // bond or site of the local update that failed
+  const char* fail_what = "";
   bool pending_init = false;  // uploaded, TDVP.__init__ not yet run
   cplx<T>* cur(int i) { return A[par[i]][i]; }
   cplx<T>* alt(int i) { return A[par[i] ^ 1][i]; }
@@ -195,12 +201,16 @@ struct EngineBase {
   virtual int add(const qca_chain_desc* d, cudaStream_t st, int* id) = 0;
   virtual int remove(int id) = 0;
   virtual int step(const int* ids, int count, int nsteps, cudaStream_t st) = 0;
+  virtual int schedule(int id, int nsteps) = 0;
+  virtual int advance(const int* ids, int count, int max_ticks, cudaStream_t st) = 0;
+  virtual int progress(int id, long long* out) = 0;
   virtual int measure(int id, double* pop, double* dpop, double* sse, double* bonds, cudaStream_t st) = 0;
   virtual int measure_many(const int* ids, int count, double* pop, double* dpop, double* sse, double* bonds,
                            cudaStream_t st) = 0;
   virtual int bonds(int id, int* out) = 0;
   virtual int get_mps(int id, double* out, size_t cap, cudaStream_t st) = 0;
   virtual int stats(int id, double* out) = 0;
+  virtual int stats_ex(int id, double* out, int count) = 0;
   virtual std::vector<int> ids() const = 0;
   virtual int kernel_stats(double* out, int reset) = 0;
   virtual int set_profile(int on) = 0;
@@ -307,7 +317,7 @@ struct Engine final : EngineBase {
     done_cap = 4096;
     QCA_CUDA(cudaMallocHost(&h_done, sizeof(int) * done_cap));
     QCA_CUDA(cudaMalloc(&d_done, sizeof(int) * done_cap));
-    QCA_CUDA(cudaMallocHost(&h_k, sizeof(int) * done_cap));
+    QCA_CUDA(cudaMallocHost(&h_k, sizeof(int) * 4 * done_cap));
     size_t fr = 0, tot = 0;
     QCA_CUDA(cudaMemGetInfo(&fr, &tot));
     budget = budget_bytes ? budget_bytes : (size_t)(0.9 * fr);
@@ -674,6 +684,7 @@ struct Engine final : EngineBase {
       d.in = p.in;
       d.P = p.c->lzP;
       d.done_out = d_done + i;
+      d.status = p.c->iflags + 3;
     }
     {
       const std::vector<Span> sp = spans();
@@ -1182,18 +1193,23 @@ struct Engine final : EngineBase {
       QCA_TRY(timed(KC_QR, 0, 0, st, [&] { return launch_qr<T>(dq, (int)qr.size(), 0, st); }));
     }
     if (!svc.empty()) {
+      if (svc.size() > (size_t)done_cap) {
+        set_error("too many simultaneous two-site splits (%zu)", svc.size());
+        return QCA_ERR_INVALID;
+      }
       for (size_t i = 0; i < svc.size(); ++i)
-        QCA_CUDA(cudaMemcpyAsync(h_k + 2 * i, svc[i]->iflags, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+        QCA_CUDA(cudaMemcpyAsync(h_k + 4 * i, svc[i]->iflags, 4 * sizeof(int), cudaMemcpyDeviceToHost, st));
       QCA_TRY(sync(st));
       for (size_t i = 0; i < svc.size(); ++i) {
         Chain<T>* c = svc[i];
         const int l = c->dir == 0 ? c->pos : c->pos - 1;
-        const int k = h_k[2 * i];
+        const int k = h_k[4 * i];
         if (k < 1 || k > c->cap[l + 1]) {
           set_error("SVD returned bond dimension %d (capacity %d)", k, c->cap[l + 1]);
           return QCA_ERR_INVALID;
         }
-        if (h_k[2 * i + 1]) c->status = h_k[2 * i + 1];
+        note_failure(c, h_k[4 * i + 1], h_k[4 * i + 3], l);
+        c->svd_sweeps = std::max(c->svd_sweeps, h_k[4 * i + 2]);
         c->D[l + 1] = k;
       }
       for (size_t i = 0; i < svc.size(); ++i) {
@@ -1328,6 +1344,8 @@ struct Engine final : EngineBase {
             c->pos = 0;
             c->todo--;
             c->center = 0;
+            c->in_step = false;
+            c->steps_done++;
           }
         }
       } else {
@@ -1346,11 +1364,53 @@ struct Engine final : EngineBase {
             c->pos = 0;
             c->todo--;
             c->center = 0;
+            c->in_step = false;
+            c->steps_done++;
           }
         }
       }
     }
     return QCA_OK;
+  }
+
+  // ------------------------------------------------------------------ failures
+  // Record the first numerical failure of a chain from its device status words:
+  // the SVD status (0, QCA_ERR_NAN, QCA_ERR_NOT_CONVERGED) and the sticky Lanczos
+  // bits (kLzStatus*).  A failed chain takes no further part in the step.
+  static void note_failure(Chain<T>* c, int svd_status, int lz_bits, int site) {
+    int code = QCA_OK;
+    const char* what = "";
+    if ((lz_bits & kLzStatusNonFinite) || svd_status == QCA_ERR_NAN) {
+      code = QCA_ERR_NAN;
+      what = "non-finite values in a local update";
+    } else if (svd_status == QCA_ERR_NOT_CONVERGED) {
+      code = QCA_ERR_NOT_CONVERGED;
+      what = "Jacobi sweeps of the two-site split ran out";
+    } else if (lz_bits & kLzStatusLimit) {
+      code = QCA_ERR_NOT_CONVERGED;
+      what = "a Lanczos exponential reached its iteration limit";
+    }
+    if (code != QCA_OK && c->status == QCA_OK) {
+      c->status = code;
+      c->fail_site = site;
+      c->fail_what = what;
+    }
+  }
+
+  // The status of a set of chains: QCA_ERR_NAN before QCA_ERR_NOT_CONVERGED, with
+  // the first failed chain named in the error message.
+  static int report_failures(const std::vector<Chain<T>*>& C) {
+    Chain<T>* worst = nullptr;
+    int nfail = 0;
+    for (auto* c : C) {
+      if (c->status == QCA_OK) continue;
+      ++nfail;
+      if (!worst || (c->status == QCA_ERR_NAN && worst->status != QCA_ERR_NAN)) worst = c;
+    }
+    if (!worst) return QCA_OK;
+    set_error("chain %d: %s (at position %d); %d chain(s) failed, the others completed the step", worst->id,
+              worst->fail_what, worst->fail_site, nfail);
+    return worst->status;
   }
 
   // ------------------------------------------------------------------ public ops
@@ -1367,41 +1427,70 @@ struct Engine final : EngineBase {
     return QCA_OK;
   }
 
-  int step(const int* ids, int count, int nsteps, cudaStream_t st) override {
+  std::vector<Chain<T>*> select(const int* ids, int count, int* status) {
     std::vector<Chain<T>*> C;
+    *status = QCA_OK;
     if (ids) {
       for (int i = 0; i < count; ++i) {
         auto it = chains.find(ids[i]);
         if (it == chains.end()) {
           set_error("unknown chain %d", ids[i]);
-          return QCA_ERR_INVALID;
+          *status = QCA_ERR_INVALID;
+          return {};
         }
         C.push_back(it->second.get());
       }
     } else {
       for (auto& kv : chains) C.push_back(kv.second.get());
     }
-    if (C.empty() || nsteps <= 0) return QCA_OK;
-    QCA_TRY(ensure_init(st));
-    // chains whose gauge was moved by a measurement: make_site_canonical(0) and
-    // rebuild the right environments (the gauge-consistent start of tdvp.py:54)
-    std::vector<Chain<T>*> dirty;
-    for (auto* c : C) {
-      c->todo = nsteps;
+    return C;
+  }
+
+  // Begin the next time step of every listed chain that has one scheduled: the
+  // gauge-consistent start of tdvp.py:50-54 (chains whose gauge a measurement
+  // moved are re-canonicalised and get their right environments rebuilt, grouped)
+  // and the per-step statistics reset.
+  int begin_steps(const std::vector<Chain<T>*>& C, cudaStream_t st) {
+    std::vector<Chain<T>*> starting, dirty;
+    for (auto* c : C)
+      if (c->todo > 0 && !c->in_step && c->status == QCA_OK) starting.push_back(c);
+    if (starting.empty()) return QCA_OK;
+    for (auto* c : starting) {
       c->dir = 0;
       c->pos = 0;
       c->lz_used = 0;
+      c->svd_sweeps = 0;
       c->disc_host = 0.0;
+      c->in_step = true;
       if (c->center != 0) dirty.push_back(c);
+      QCA_CUDA(cudaMemsetAsync(c->dscal, 0, sizeof(double), st));
+      QCA_CUDA(cudaMemsetAsync(c->iflags + 3, 0, sizeof(int), st));
     }
-    for (auto* c : C) QCA_CUDA(cudaMemsetAsync(c->dscal, 0, sizeof(double), st));
     if (!dirty.empty()) QCA_TRY(canonicalize_right(dirty, false, st));
-    while (true) {
+    return QCA_OK;
+  }
+
+  // Up to max_ticks lock-step ticks (one local update of every chain in a step),
+  // starting scheduled steps as chains become free, so that a chain that finishes
+  // a time step begins its next one at the following tick (continuous batching).
+  // Then the failure bits of the local updates since the last per-tick check are
+  // read (1TDVP chains, the backward evolutions after a chain's last split).
+  int run_ticks(const std::vector<Chain<T>*>& C, long long max_ticks, cudaStream_t st) {
+    QCA_TRY(ensure_init(st));
+    for (long long t = 0; t < max_ticks; ++t) {
+      QCA_TRY(begin_steps(C, st));
       std::vector<Chain<T>*> act;
       for (auto* c : C)
-        if (c->todo > 0) act.push_back(c);
+        if (c->in_step && c->status == QCA_OK) act.push_back(c);
       if (act.empty()) break;
       QCA_TRY(tick(act, st));
+    }
+    for (size_t b = 0; b < C.size(); b += (size_t)done_cap) {
+      const size_t e = std::min(C.size(), b + (size_t)done_cap);
+      for (size_t i = b; i < e; ++i)
+        QCA_CUDA(cudaMemcpyAsync(h_k + 4 * (i - b), C[i]->iflags, 4 * sizeof(int), cudaMemcpyDeviceToHost, st));
+      QCA_TRY(sync(st));
+      for (size_t i = b; i < e; ++i) note_failure(C[i], QCA_OK, h_k[4 * (i - b) + 3], -1);
     }
     QCA_TRY(sync(st));
     if (std::is_same<T, float>::value && use_tc && use_umma) {
@@ -1411,6 +1500,75 @@ struct Engine final : EngineBase {
         set_error("tensor-core GEMM: %d mbarrier waits ran out", timeouts);
         return QCA_ERR_CUDA;
       }
+    }
+    return QCA_OK;
+  }
+
+  int step(const int* ids, int count, int nsteps, cudaStream_t st) override {
+    int s = QCA_OK;
+    std::vector<Chain<T>*> C = select(ids, count, &s);
+    if (s != QCA_OK) return s;
+    if (C.empty() || nsteps <= 0) return QCA_OK;
+    for (auto* c : C) {
+      if (c->status != QCA_OK) {
+        set_error("chain %d failed in an earlier step (%s at position %d); remove it", c->id, c->fail_what,
+                  c->fail_site);
+        return c->status;
+      }
+      if (c->in_step || c->todo > 0) {
+        set_error("chain %d has time steps scheduled by qca_engine_advance; finish them first", c->id);
+        return QCA_ERR_INVALID;
+      }
+    }
+    for (auto* c : C) c->todo = nsteps;
+    QCA_TRY(run_ticks(C, std::numeric_limits<long long>::max(), st));
+    return report_failures(C);
+  }
+
+  int schedule(int id, int nsteps) override {
+    auto it = chains.find(id);
+    if (it == chains.end()) {
+      set_error("unknown chain %d", id);
+      return QCA_ERR_INVALID;
+    }
+    if (nsteps < 0) {
+      set_error("qca_chain_schedule: negative step count");
+      return QCA_ERR_INVALID;
+    }
+    it->second->todo += nsteps;
+    return QCA_OK;
+  }
+
+  int advance(const int* ids, int count, int max_ticks, cudaStream_t st) override {
+    int s = QCA_OK;
+    std::vector<Chain<T>*> C = select(ids, count, &s);
+    if (s != QCA_OK) return s;
+    std::vector<Chain<T>*> live;
+    for (auto* c : C)
+      if (c->status == QCA_OK) live.push_back(c);
+    if (live.empty() || max_ticks <= 0) return QCA_OK;
+    QCA_TRY(run_ticks(live, max_ticks, st));
+    return report_failures(live);
+  }
+
+  int progress(int id, long long* out) override {
+    auto it = chains.find(id);
+    if (it == chains.end()) {
+      set_error("unknown chain %d", id);
+      return QCA_ERR_INVALID;
+    }
+    const Chain<T>* c = it->second.get();
+    out[0] = c->steps_done;
+    out[1] = c->todo;
+    out[2] = c->in_step ? 1 : 0;
+    out[3] = c->status;
+    return QCA_OK;
+  }
+
+  int check_boundary(const Chain<T>* c, const char* what) const {
+    if (c->in_step) {
+      set_error("%s: chain %d is inside a time step (qca_engine_advance stopped mid-sweep)", what, c->id);
+      return QCA_ERR_INVALID;
     }
     return QCA_OK;
   }
@@ -1429,6 +1587,7 @@ struct Engine final : EngineBase {
         return QCA_ERR_INVALID;
       }
       C.push_back(it->second.get());
+      QCA_TRY(check_boundary(C.back(), "qca_engine_measure"));
     }
     QCA_TRY(ensure_init(st));
     size_t ob = 0;
@@ -1579,6 +1738,7 @@ struct Engine final : EngineBase {
       return QCA_ERR_INVALID;
     }
     Chain<T>* c = it->second.get();
+    QCA_TRY(check_boundary(c, "qca_chain_get_mps"));
     QCA_TRY(ensure_init(st));
     size_t need = 0;
     for (int i = 0; i < c->N; ++i) need += 4ull * c->D[i] * c->D[i + 1];
@@ -1613,6 +1773,15 @@ struct Engine final : EngineBase {
     QCA_CUDA(cudaMemcpy(&disc, c->dscal, sizeof(double), cudaMemcpyDeviceToHost));
     out[0] = c->lz_used;
     out[1] = disc;
+    return QCA_OK;
+  }
+
+  int stats_ex(int id, double* out, int count) override {
+    double base[2];
+    QCA_TRY(stats(id, base));
+    const Chain<T>* c = chains.find(id)->second.get();
+    const double all[5] = {base[0], base[1], (double)c->svd_sweeps, (double)c->status, (double)c->bytes};
+    for (int i = 0; i < count && i < 5; ++i) out[i] = all[i];
     return QCA_OK;
   }
 
@@ -1956,6 +2125,30 @@ int qca_engine_step_chains(qca_engine* e, const int* chain_ids, int count, int n
   return e->impl->step(chain_ids, count, nsteps, (cudaStream_t)stream);
 }
 
+int qca_chain_schedule(qca_engine* e, int chain_id, int nsteps) {
+  if (!e) {
+    set_error("qca_chain_schedule: NULL engine");
+    return QCA_ERR_INVALID;
+  }
+  return e->impl->schedule(chain_id, nsteps);
+}
+
+int qca_engine_advance(qca_engine* e, const int* chain_ids, int count, int max_ticks, void* stream) {
+  if (!e || count < 0 || (count > 0 && !chain_ids)) {
+    set_error("qca_engine_advance: invalid arguments");
+    return QCA_ERR_INVALID;
+  }
+  return e->impl->advance(count > 0 ? chain_ids : nullptr, count, max_ticks, (cudaStream_t)stream);
+}
+
+int qca_chain_progress(qca_engine* e, int chain_id, long long* progress) {
+  if (!e || !progress) {
+    set_error("qca_chain_progress: NULL argument");
+    return QCA_ERR_INVALID;
+  }
+  return e->impl->progress(chain_id, progress);
+}
+
 int qca_chain_measure(qca_engine* e, int chain_id, double* population, double* d_population,
                       double* single_site_entropy, double* bond_dims, void* stream) {
   if (!e) {
@@ -2013,6 +2206,14 @@ int qca_chain_stats(qca_engine* e, int chain_id, double* stats) {
     return QCA_ERR_INVALID;
   }
   return e->impl->stats(chain_id, stats);
+}
+
+int qca_chain_stats_ex(qca_engine* e, int chain_id, double* stats, int count) {
+  if (!e || !stats || count < 0) {
+    set_error("qca_chain_stats_ex: invalid arguments");
+    return QCA_ERR_INVALID;
+  }
+  return e->impl->stats_ex(chain_id, stats, count);
 }
 
 }  // extern "C"

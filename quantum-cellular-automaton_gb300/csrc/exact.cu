@@ -751,6 +751,7 @@ int noalloc_setup(void** addr) {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) {
+      cudaGetLastError();  // clear it, so that no later launch check reports it
       set_error("qca_exact_step_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
       return QCA_ERR_CUDA;
     }

@@ -119,6 +119,7 @@ __global__ void __launch_bounds__(kLzThreads) lz_init_kernel(const LanczosDesc<T
     D.S[LZ_MEFF] = 1.0;
     D.S[LZ_INVB] = 0.0;
     D.S[LZ_FLAG] = isfinite(nrm) ? 0.0 : 1.0;
+    if (!isfinite(nrm) && D.status) atomicOr(D.status, kLzStatusNonFinite);
     D.S[LZ_TOL] = tol;
     D.S[LZ_COEF] = nrm;  // exp of an empty Krylov space: v itself
     D.S[LZ_COEF + 1] = 0.0;
@@ -273,6 +274,7 @@ __global__ void lz_finalize_kernel(const LanczosDesc<T>* __restrict__ descs, int
       S[LZ_MEFF] = (double)m;
       *done = 1;
       if (D.done_out) *D.done_out = 1;
+      if (D.status) atomicOr(D.status, kLzStatusNonFinite);
     }
     return;
   }
@@ -346,8 +348,12 @@ __global__ void lz_finalize_kernel(const LanczosDesc<T>* __restrict__ descs, int
     if (!finite) {
       S[LZ_FLAG] = 1.0;
       *done = 1;
+      if (D.status) atomicOr(D.status, kLzStatusNonFinite);
     } else if (err < tol || beta < 1e-300 || m + 1 > mmax || m + 1 > kLzMax) {
-      if (!(err < tol) && !(beta < 1e-300)) S[LZ_FLAG] = 2.0;  // iteration limit reached
+      if (!(err < tol) && !(beta < 1e-300)) {
+        S[LZ_FLAG] = 2.0;  // iteration limit reached
+        if (D.status) atomicOr(D.status, kLzStatusLimit);
+      }
       *done = 1;
     } else if (beta < tol * 1e-3) {
       *done = 1;  // invariant subspace: T is exact

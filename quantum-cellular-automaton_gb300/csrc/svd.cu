@@ -25,8 +25,9 @@
 //    every round of a round-robin tournament rotates one disjoint column pair per
 //    warp through distributed shared memory, and the cluster barrier separates the
 //    rounds.
-// Column norms are evaluated at the start of every sweep (block round) and updated
-// in closed form by each rotation (a' = a - t|g|, b' = b + t|g|).
+// Every rotation evaluates the pair's squared norms and inner product afresh from
+// the columns (one pass, one shuffle tree), so the rotation angles never rest on
+// drifted norms and the sweeps keep their quadratic convergence.
 #include <cooperative_groups.h>
 
 #include <algorithm>
@@ -46,6 +47,23 @@ constexpr int kSvdMaxSweeps = 24;
 constexpr int kSvdBlk = 16;              // columns per block of svd_block_kernel
 constexpr size_t kSvdSmem = 200 * 1024;  // dynamic shared memory per CTA
 
+// Rotation tolerance on |u^H v| / (||u|| ||v||).  It must sit clearly above the
+// rounding noise of the inner product, or pairs whose true inner product is below
+// the noise keep rotating and the sweeps never terminate: FP64 sums over mx
+// elements carry up to ~mx eps of noise, hence mx eps (at least 8 eps); the FP32
+// inner products (at most 16 elements per lane, then a 5-level tree) carry a few
+// eps32, hence 16 eps32.
+template <typename T>
+__device__ __forceinline__ double jacobi_tol(int mx) {
+  return sizeof(T) == 4 ? 16.0 * 1.2e-7 : 2.2e-16 * fmax(8.0, (double)mx);
+}
+
+// Jacobi sweep limit of a problem (the descriptor may lower the default)
+template <typename T>
+__device__ __forceinline__ int svd_max_sweeps(const SvdDesc<T>& D) {
+  return D.max_sweeps > 0 && D.max_sweeps < kSvdMaxSweeps ? D.max_sweeps : kSvdMaxSweeps;
+}
+
 template <typename T>
 struct Prec;
 template <>
@@ -57,11 +75,9 @@ struct Prec<float> {
   static constexpr double eps = 1.2e-7;
 };
 
-// Gram entries of a column pair: ||u||^2, ||v||^2 and u^H v.  In FP32 the sums are
-// compensated (each product split exactly with an FMA, partial sums carried as
-// hi + lo pairs, also through the warp reduction), so that small inner products of
-// nearly orthogonal columns are resolved beyond the sqrt(m) eps32 noise of a plain
-// FP32 sum and the rotations can drive the columns to FP32-level orthogonality.
+// Compensated FP32 sums (each product split exactly with an FMA, partial sums
+// carried as hi + lo pairs, also through the warp reduction) for the column norms
+// that decide the singular values and the rounding floor.
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   s = a + b;
   const float bb = s - a;
@@ -90,52 +106,7 @@ struct DF {
   __device__ __forceinline__ float value() const { return hi + lo; }
 };
 
-// Warp-wide sums over the RPL elements each lane holds: the pair's inner product in
-// the working precision (each lane sums at most 16 elements, then a 5-level tree,
-// which keeps the FP32 error at a few eps32 |u||v|, below the FP32 rotation
-// tolerance of 16 eps32); the squared column norms compensated in FP32 (products
-// split exactly with an FMA, partial sums carried as hi + lo pairs, also through the
-// warp reduction).  Every lane returns lane 0's result, so that all lanes of a warp
-// take the same branch and apply the same rotation.
-template <typename T, int RPL>
-__device__ __forceinline__ void pair_cross(const cplx<T> (&ru)[RPL], const cplx<T> (&rv)[RPL], T& gr, T& gi) {
-  if constexpr (sizeof(T) == 4) {
-    // plain FP32: each lane sums only RPL <= 16 elements, then a 5-level tree, so
-    // the error stays a few eps32 |u||v|, below the rotation tolerance of 16 eps32
-    float r = 0.f, i = 0.f;
-#pragma unroll
-    for (int k = 0; k < RPL; ++k) {
-      const cplx<T> u = ru[k], v = rv[k];
-      r = fmaf(u.re, v.re, fmaf(u.im, v.im, r));  // conj(u) v
-      i = fmaf(u.re, v.im, fmaf(-u.im, v.re, i));
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      r += __shfl_xor_sync(0xffffffffu, r, o);
-      i += __shfl_xor_sync(0xffffffffu, i, o);
-    }
-    gr = r;
-    gi = i;
-  } else {
-    T r = 0, i = 0;
-#pragma unroll
-    for (int k = 0; k < RPL; ++k) {
-      const cplx<T> u = ru[k], v = rv[k];
-      r = fma(u.re, v.re, fma(u.im, v.im, r));
-      i = fma(u.re, v.im, fma(-u.im, v.re, i));
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      r += __shfl_xor_sync(0xffffffffu, r, o);
-      i += __shfl_xor_sync(0xffffffffu, i, o);
-    }
-    gr = r;
-    gi = i;
-  }
-  gr = __shfl_sync(0xffffffffu, gr, 0);
-  gi = __shfl_sync(0xffffffffu, gi, 0);
-}
-
+// Squared norm of one column held in the registers of a warp (compensated in FP32).
 template <typename T, int RPL>
 __device__ __forceinline__ T col_norm2(const cplx<T> (&ru)[RPL]) {
   T a;
@@ -179,8 +150,43 @@ __device__ __forceinline__ void col_store(cplx<T>* p, int len, const cplx<T> (&r
   }
 }
 
+// Gram entries of a column pair from the registers of a warp: ||u||^2, ||v||^2 and
+// u^H v, each lane summing its RPL <= 16 elements in the working precision, then
+// one 5-level shuffle tree for the four sums (error a few eps |u||v|, below the
+// rotation tolerance).  Every lane returns lane 0's values, so that all lanes of a
+// warp take the same branch and apply the same rotation.
+template <typename T, int RPL>
+__device__ __forceinline__ void pair_gram(const cplx<T> (&ru)[RPL], const cplx<T> (&rv)[RPL], T& au, T& bv, T& gr,
+                                          T& gi) {
+  T a = 0, b = 0, r = 0, i = 0;
+#pragma unroll
+  for (int k = 0; k < RPL; ++k) {
+    const cplx<T> u = ru[k], v = rv[k];
+    a = fma(u.re, u.re, fma(u.im, u.im, a));
+    b = fma(v.re, v.re, fma(v.im, v.im, b));
+    r = fma(u.re, v.re, fma(u.im, v.im, r));  // conj(u) v
+    i = fma(u.re, v.im, fma(-u.im, v.re, i));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+    r += __shfl_xor_sync(0xffffffffu, r, o);
+    i += __shfl_xor_sync(0xffffffffu, i, o);
+  }
+  au = __shfl_sync(0xffffffffu, a, 0);
+  bv = __shfl_sync(0xffffffffu, b, 0);
+  gr = __shfl_sync(0xffffffffu, r, 0);
+  gi = __shfl_sync(0xffffffffu, i, 0);
+}
+
 // One Jacobi rotation of the column pair (xu, xv) of X, applied to (vu, vv) of V,
-// all held in registers; al, be are the squared column norms on entry and exit.
+// all held in registers.  The squared column norms and the inner product are
+// evaluated afresh from the registers for every pair: norms carried from earlier
+// rotations in closed form drift (by the rounding of every update, and badly after
+// cancellation), and a rotation angle computed from drifted norms leaves an inner
+// product of the size of the drift, which turns the quadratic convergence of the
+// sweeps into a linear one.  al, be return the new squared norms (closed form).
 // Returns false (nothing changed) when the pair is already orthogonal to the
 // tolerance or one column is at the rounding floor of the matrix.
 //   x_p' = c x_p - s e^{-i phi} x_q ;  x_q' = s e^{i phi} x_p + c x_q   (unitary)
@@ -188,7 +194,7 @@ template <typename T, int RPL>
 __device__ __forceinline__ bool jacobi_rotate(cplx<T> (&xu)[RPL], cplx<T> (&xv)[RPL], cplx<T> (&vu)[RPL],
                                               cplx<T> (&vv)[RPL], T& al, T& be, double tol, T floor2) {
   T gr, gi;
-  pair_cross<T, RPL>(xu, xv, gr, gi);
+  pair_gram<T, RPL>(xu, xv, al, be, gr, gi);
   const T g = sqrt(gr * gr + gi * gi);
   if (!(g > (T)tol * sqrt(al * be)) || al <= floor2 || be <= floor2) return false;
   const T zeta = (be - al) / (2 * g);
@@ -207,14 +213,8 @@ __device__ __forceinline__ bool jacobi_rotate(cplx<T> (&xu)[RPL], cplx<T> (&xv)[
     vu[r] = c * va + smq * vb;
     vv[r] = spq * va + c * vb;
   }
-  T aln = al - t * g, ben = be + t * g;
-  if (aln < (T)0.01 * al || ben < (T)0.01 * be) {
-    // cancellation in the closed-form update: re-evaluate from the rotated columns
-    aln = col_norm2<T, RPL>(xu);
-    ben = col_norm2<T, RPL>(xv);
-  }
-  al = aln;
-  be = ben;
+  al = fmax(al - t * g, (T)0);
+  be = fmax(be + t * g, (T)0);
   return true;
 }
 
@@ -253,10 +253,22 @@ __device__ void svd_finish(const SvdDesc<T>& D, cg::cluster_group& cluster, int 
     double s = 0.0;
     for (int i = lane; i < mx; i += 32) s += (double)x[i].re * x[i].re + (double)x[i].im * x[i].im;
     s = warp_sum(s);
-    if (lane == 0) snorm0[j] = sqrt(s);
+    // a non-finite column is marked (-1) and ranked as zero, so that the rank
+    // permutation below stays a permutation; the problem reports QCA_ERR_NAN
+    if (lane == 0) snorm0[j] = isfinite(s) ? sqrt(s) : -1.0;
   }
   cluster.sync();
   if (rank == 0) {
+    if (threadIdx.x == 0) *s_k = 0;
+    __syncthreads();
+    for (int j = threadIdx.x; j < nx; j += blockDim.x)
+      if (!(snorm[j] >= 0.0)) {
+        snorm[j] = 0.0;
+        *s_k = 1;
+      }
+    __syncthreads();
+    const bool non_finite = *s_k != 0;
+    __syncthreads();
     for (int j = threadIdx.x; j < nx; j += blockDim.x) {
       const double sj = snorm[j];
       int r = 0;
@@ -295,7 +307,7 @@ __device__ void svd_finish(const SvdDesc<T>& D, cg::cluster_group& cluster, int 
       if (D.discarded) *D.discarded += total > 0 ? (total - keep) / total : 0.0;
       for (int i = 0; i < nx; ++i) D.sv[i] = snorm[perm[i]];
       if (D.status) {
-        D.status[0] = (sweep >= kSvdMaxSweeps) ? QCA_ERR_NOT_CONVERGED : 0;
+        D.status[0] = non_finite ? QCA_ERR_NAN : (sweep >= svd_max_sweeps(D)) ? QCA_ERR_NOT_CONVERGED : 0;
         D.status[1] = sweep + 1;  // sweeps used
       }
     }
@@ -387,7 +399,6 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
   __shared__ double s_keep;
   __shared__ double s_fro;  // ||Theta||_F^2 (CTA 0)
   __shared__ double red[33];
-  __shared__ T s_cn[kSvdMaxN];  // squared norms of this CTA's columns
   const int m = 2 * D.Dl, n = 2 * D.Dr;
   const bool trans = n > m;
   const int mx = trans ? n : m;
@@ -420,21 +431,14 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
   const double fro = *cluster.map_shared_rank(&s_fro, 0);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int P = nx + (nx & 1);
-  const double tol = Prec<T>::eps * (sizeof(T) == 4 ? 16.0 : fmax(8.0, 2.0 * sqrt((double)mx)));
+  const double tol = jacobi_tol<T>(mx);
   const T floor2 = (T)(16.0 * Prec<T>::eps * Prec<T>::eps * fro);
   int* flag0 = cluster.map_shared_rank(s_flag, 0);
   int sweep = 0;
-  for (; sweep < kSvdMaxSweeps; ++sweep) {
+  const int max_sweeps = svd_max_sweeps(D);
+  for (; sweep < max_sweeps; ++sweep) {
     const int par = sweep & 1;
     int rotated = 0;
-    for (int lc = wid; lc < cpc; lc += nw) {
-      if (rank * cpc + lc >= nx) break;
-      cplx<T> ru[RPL];
-      col_load<T, RPL>(Xloc + (long long)lc * mx, mx, ru);
-      const T a = col_norm2<T, RPL>(ru);
-      if (lane == 0) s_cn[lc] = a;
-    }
-    cluster.sync();
     for (int round = 0; round < P - 1; ++round) {
       for (int pk = rank + cs * wid; pk < P / 2; pk += cs * nw) {
         int p, q;
@@ -457,8 +461,6 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
                               : D.work + (long long)(p / cpc) * cpc * nx) + (long long)(p % cpc) * nx;
         cplx<T>* vq = (v_smem ? cluster.map_shared_rank(Xloc, q / cpc) + (long long)cpc * mx
                               : D.work + (long long)(q / cpc) * cpc * nx) + (long long)(q % cpc) * nx;
-        T* cnp = cluster.map_shared_rank(s_cn, p / cpc) + (p % cpc);
-        T* cnq = cluster.map_shared_rank(s_cn, q / cpc) + (q % cpc);
         // both columns of X and of V staged in registers in one round of (possibly
         // remote) loads; the rotation in the working precision T (the singular values
         // are re-evaluated in FP64 after convergence)
@@ -467,17 +469,13 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
         col_load<T, RPL>(xq, mx, rv);
         col_load<T, RPL>(vp, nx, wu);
         col_load<T, RPL>(vq, nx, wv);
-        T al = *cnp, be = *cnq;
+        T al, be;
         if (!jacobi_rotate<T, RPL>(ru, rv, wu, wv, al, be, tol, floor2)) continue;
         rotated = 1;
         col_store<T, RPL>(xp, mx, ru);
         col_store<T, RPL>(xq, mx, rv);
         col_store<T, RPL>(vp, nx, wu);
         col_store<T, RPL>(vq, nx, wv);
-        if (lane == 0) {
-          *cnp = al;
-          *cnq = be;
-        }
       }
       cluster.sync();
     }
@@ -506,7 +504,6 @@ __global__ void __launch_bounds__(kSvdThreads) svd_block_kernel(const SvdDesc<T>
   __shared__ double s_keep;
   __shared__ double s_fro;  // ||Theta||_F^2 (CTA 0)
   __shared__ double red[33];
-  __shared__ T s_cn[2][kSvdBlk];  // squared norms of the resident columns
   const int m = 2 * D.Dl, n = 2 * D.Dr;
   const bool trans = n > m;
   const int mx = trans ? n : m;
@@ -552,23 +549,16 @@ __global__ void __launch_bounds__(kSvdThreads) svd_block_kernel(const SvdDesc<T>
   cluster.sync();
   const double fro = *cluster.map_shared_rank(&s_fro, 0);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const double tol = Prec<T>::eps * (sizeof(T) == 4 ? 16.0 : fmax(8.0, 2.0 * sqrt((double)mx)));
+  const double tol = jacobi_tol<T>(mx);
   const T floor2 = (T)(16.0 * Prec<T>::eps * Prec<T>::eps * fro);
   int* flag0 = cluster.map_shared_rank(s_flag, 0);
   int gen = 0, sweep = 0;
-  for (; sweep < kSvdMaxSweeps; ++sweep) {
+  const int max_sweeps = svd_max_sweeps(D);
+  for (; sweep < max_sweeps; ++sweep) {
     const int par = sweep & 1;
     int rotated = 0;
     for (int r = 0; r < n2 - 1; ++r) {
       const int bt = player(rank, r), bb = player(n2 - 1 - rank, r);
-      for (int c = wid; c < 2 * b; c += nw) {
-        const int s = c / b, j = c - s * b;
-        cplx<T> ru[RPL];
-        col_load<T, RPL>(xs(gen, s, j), mx, ru);
-        const T a = col_norm2<T, RPL>(ru);
-        if (lane == 0) s_cn[s][j] = a;
-      }
-      __syncthreads();
       if (r == 0) {
         // pairs inside each resident block, both blocks at once (round robin over b)
         const int Bp = b + (b & 1), half = Bp / 2;
@@ -592,17 +582,13 @@ __global__ void __launch_bounds__(kSvdThreads) svd_block_kernel(const SvdDesc<T>
             col_load<T, RPL>(xs(gen, s, q), mx, xv);
             col_load<T, RPL>(vc(gen, s, p, gp), nx, vu);
             col_load<T, RPL>(vc(gen, s, q, gq), nx, vv);
-            T al = s_cn[s][p], be = s_cn[s][q];
+            T al, be;
             if (!jacobi_rotate<T, RPL>(xu, xv, vu, vv, al, be, tol, floor2)) continue;
             rotated = 1;
             col_store<T, RPL>(xs(gen, s, p), mx, xu);
             col_store<T, RPL>(xs(gen, s, q), mx, xv);
             col_store<T, RPL>(vc(gen, s, p, gp), nx, vu);
             col_store<T, RPL>(vc(gen, s, q, gq), nx, vv);
-            if (lane == 0) {
-              s_cn[s][p] = al;
-              s_cn[s][q] = be;
-            }
           }
           __syncthreads();
         }
@@ -617,7 +603,6 @@ __global__ void __launch_bounds__(kSvdThreads) svd_block_kernel(const SvdDesc<T>
         if (act) {
           col_load<T, RPL>(xs(gen, 0, wid), mx, xu);
           col_load<T, RPL>(vc(gen, 0, wid, ga), nx, vu);
-          al = s_cn[0][wid];
         }
         bool dirty = false;
         for (int i = 0; i < b; ++i) {
@@ -628,13 +613,12 @@ __global__ void __launch_bounds__(kSvdThreads) svd_block_kernel(const SvdDesc<T>
               cplx<T> xv[RPL], vv[RPL];
               col_load<T, RPL>(xs(gen, 1, j), mx, xv);
               col_load<T, RPL>(vc(gen, 1, j, gb), nx, vv);
-              T be = s_cn[1][j];
+              T be;
               if (jacobi_rotate<T, RPL>(xu, xv, vu, vv, al, be, tol, floor2)) {
                 rotated = 1;
                 dirty = true;
                 col_store<T, RPL>(xs(gen, 1, j), mx, xv);
                 col_store<T, RPL>(vc(gen, 1, j, gb), nx, vv);
-                if (lane == 0) s_cn[1][j] = be;
               }
             }
           }
@@ -850,8 +834,8 @@ template int svd_cluster_size<float>(int, int);
 // values in descending order; *k_out the truncated bond (right-sweep form: A_l = U,
 // A_r = s Vh / ||s||).  Synchronises the stream.
 template <typename T>
-static int test_svd(int Dl, int Dr, const void* theta, int chi, double eps, void* Al, void* Ar, double* sv,
-                    int* k_out, cudaStream_t st) {
+static int test_svd(int Dl, int Dr, const void* theta, int chi, double eps, int max_sweeps, void* Al, void* Ar,
+                    double* sv, int* k_out, cudaStream_t st) {
   using namespace qca;
   const int m = 2 * Dl, n = 2 * Dr, mx = std::max(m, n), nx = std::min(m, n);
   void* scratch = nullptr;
@@ -868,6 +852,7 @@ static int test_svd(int Dl, int Dr, const void* theta, int chi, double eps, void
   d.kmax = nx;
   d.eps = eps;
   d.right_sweep = 1;
+  d.max_sweeps = max_sweeps;
   d.Al = (cplx<T>*)Al;
   d.Ar = (cplx<T>*)Ar;
   d.work = (cplx<T>*)base;
@@ -894,6 +879,10 @@ static int test_svd(int Dl, int Dr, const void* theta, int chi, double eps, void
   cudaFree(scratch);
   if (s != QCA_OK) return s;
   *k_out = h[0];
+  if (h[1] == QCA_ERR_NAN) {
+    set_error("qca_test_svd: non-finite singular values");
+    return QCA_ERR_NAN;
+  }
   if (h[1] != 0) {
     set_error("qca_test_svd: Jacobi sweeps did not converge (%d sweeps)", h[2]);
     return QCA_ERR_NOT_CONVERGED;
@@ -901,17 +890,29 @@ static int test_svd(int Dl, int Dr, const void* theta, int chi, double eps, void
   return QCA_OK;
 }
 
-extern "C" int qca_test_svd(int precision, int Dl, int Dr, const void* theta, int chi, double eps, void* Al, void* Ar,
-                            double* sv, int* k_out, void* stream) {
+static int test_svd_any(int precision, int Dl, int Dr, const void* theta, int chi, double eps, int max_sweeps, void* Al,
+                        void* Ar, double* sv, int* k_out, void* stream) {
   using namespace qca;
   if (Dl < 1 || Dr < 1 || 2 * std::min(Dl, Dr) > 1024 || 2 * std::max(Dl, Dr) > 512 || !theta || !Al || !Ar ||
-      !sv || !k_out || chi < 1 || !(eps >= 0)) {
+      !sv || !k_out || chi < 1 || !(eps >= 0) || max_sweeps < 0) {
     set_error("qca_test_svd: invalid arguments");
     return QCA_ERR_INVALID;
   }
   cudaStream_t st = (cudaStream_t)stream;
-  if (precision == QCA_PREC_FP64) return test_svd<double>(Dl, Dr, theta, chi, eps, Al, Ar, sv, k_out, st);
-  if (precision == QCA_PREC_MIXED) return test_svd<float>(Dl, Dr, theta, chi, eps, Al, Ar, sv, k_out, st);
+  if (precision == QCA_PREC_FP64)
+    return test_svd<double>(Dl, Dr, theta, chi, eps, max_sweeps, Al, Ar, sv, k_out, st);
+  if (precision == QCA_PREC_MIXED)
+    return test_svd<float>(Dl, Dr, theta, chi, eps, max_sweeps, Al, Ar, sv, k_out, st);
   set_error("qca_test_svd: unknown precision %d", precision);
   return QCA_ERR_INVALID;
+}
+
+extern "C" int qca_test_svd(int precision, int Dl, int Dr, const void* theta, int chi, double eps, void* Al, void* Ar,
+                            double* sv, int* k_out, void* stream) {
+  return test_svd_any(precision, Dl, Dr, theta, chi, eps, 0, Al, Ar, sv, k_out, stream);
+}
+
+extern "C" int qca_test_svd_sweeps(int precision, int Dl, int Dr, const void* theta, int chi, double eps,
+                                   int max_sweeps, void* Al, void* Ar, double* sv, int* k_out, void* stream) {
+  return test_svd_any(precision, Dl, Dr, theta, chi, eps, max_sweeps, Al, Ar, sv, k_out, stream);
 }

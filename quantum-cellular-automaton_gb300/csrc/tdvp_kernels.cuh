@@ -93,7 +93,12 @@ struct LanczosDesc {
   const cplx<T>* in; // source vector (copied + normalised into slot 0)
   double* P;         // partial sums: 2 buffers x chunks x (2 kLzMax + 2)
   int* done_out;     // copy of the done flag for the host
+  int* status;       // sticky failure bits of the owning chain (kLzStatus*), may be null
 };
+
+// failure bits a Lanczos exponential ORs into LanczosDesc::status
+constexpr int kLzStatusNonFinite = 1;  // non-finite norm or Krylov matrix
+constexpr int kLzStatusLimit = 2;      // iteration limit reached before the tolerance
 
 constexpr int kLzMax = 48;        // largest Krylov dimension
 constexpr int kLzChunk = 2048;    // elements per CTA in the vector kernels
@@ -145,7 +150,8 @@ struct SvdDesc {
   double* sv;            // singular values (n_x), FP64
   int* k_out;            // new bond dimension
   double* discarded;     // discarded weight accumulator (+= sum of dropped s^2 / sum s^2)
-  int* status;           // [0]: 0 ok / QCA_ERR_NOT_CONVERGED, [1]: Jacobi sweeps used
+  int* status;           // [0]: 0 ok / QCA_ERR_NOT_CONVERGED / QCA_ERR_NAN, [1]: Jacobi sweeps used
+  int max_sweeps;        // Jacobi sweep limit (0: the default, 24)
 };
 
 template <typename T>

@@ -1,19 +1,21 @@
 """Continuous-batching serving loop for TDVP evolution jobs on one GPU.
 
 A job is (rule, N, initial product state, dt, steps, bond cap, algorithm).
-Jobs are admitted as device memory frees up: each chain's footprint comes
-from ``qca_chain_footprint`` (it grows as chi^2 N w) and the sum stays within
-the HBM budget.  Every scheduling round advances every resident job by one
-time step in the same grouped launches (the engine's lock-step ticks), so jobs
-that arrive while others run join the next round and their work overlaps on
-the device.  <n_i> is streamed back every ``stream_every`` steps and at the end
-of each job through ``on_populations(job_id, step, populations)``.  A round steps
-the resident jobs in groups of at most ``group`` (one engine call each); with a
-deadline, the groups left when it passes wait for the next round, so a bounded
-run overruns its wall time by at most one group step.  The callbacks run on a
-completion thread (the submission thread drives the engine alone), so user code
-that consumes the streamed populations overlaps with the next round on the GPU;
-``close()`` (called at the end of ``run``) drains it.
+Jobs are admitted as device memory frees up: each chain's footprint comes from
+``qca_chain_footprint`` (it grows as chi^2 N w) and the sum stays within the HBM
+budget.  Admitted jobs get ``stream_every`` time steps scheduled on the engine
+(``qca_chain_schedule``); every scheduling round runs a bounded number of
+lock-step ticks (``qca_engine_advance``: one local update of every resident job
+per tick, all jobs in the same grouped launches).  A job that completes its
+scheduled steps idles only until the end of the round, where its populations are
+measured and streamed and its next steps are scheduled, so long and short jobs,
+and jobs of small and large bond dimension, progress at their own pace and new
+jobs join at any round (continuous batching at local-update granularity).
+<n_i> is streamed every ``stream_every`` steps and at the end of each job through
+``on_populations(job_id, step, populations)`` on a completion thread, so user code
+that consumes the populations overlaps with the next round on the GPU.  A job
+that fails numerically (QCA_ERR_NAN / QCA_ERR_NOT_CONVERGED) is retired with its
+error and does not stop the others.
 
 This replaces the reference's per-state driver loop (``quantum_game.py:28-119``:
 one initial state at a time, measure every plot interval) with a multi-job
@@ -43,21 +45,23 @@ class JobState:
     admitted: float = 0.0
     finished: float = 0.0
     chain: int = -1
-    steps_done: int = 0
+    steps_done: int = 0       # steps completed and streamed
+    scheduled_to: int = 0     # step count the engine has been asked to reach
     bytes: int = 0
+    error: str | None = None
     stream: list = field(default_factory=list)
 
 
 class Server:
     def __init__(self, precision: str = "mixed", hbm_budget_bytes: int = 150 << 30, stream_every: int = 10,
-                 max_resident: int = 512, on_populations=None, group: int | None = None) -> None:
+                 max_resident: int = 512, on_populations=None, ticks_per_round: int = 32) -> None:
         self.precision = _lib.QCA_PREC_MIXED if precision == "mixed" else _lib.QCA_PREC_FP64
         self.engine = _Engine(self.precision, hbm_budget_bytes)
         self.budget = hbm_budget_bytes
         self.used = 0
         self.stream_every = stream_every
         self.max_resident = max_resident
-        self.group = group if group is not None else max_resident
+        self.ticks_per_round = ticks_per_round
         self.on_populations = on_populations
         self._done_q: queue.Queue | None = None
         self._done_thread: threading.Thread | None = None
@@ -65,10 +69,12 @@ class Server:
         self.pending: deque[JobState] = deque()
         self.active: list[JobState] = []
         self.done: list[JobState] = []
+        self.failed: list[JobState] = []
         self._next_id = 0
         self.site_updates = 0
         self.round_times: list[float] = []      # wall time of every scheduling round
         self.first_stream: list[float] = []     # arrival -> first streamed <n_i> per job
+        self.max_overlap = 0                    # most jobs resident in one round
 
     # ------------------------------------------------------------------ requests
     def submit(self, spec: ChainSpec, arrival: float | None = None) -> int:
@@ -83,6 +89,12 @@ class Server:
         size = ctypes.c_size_t()
         _lib.call("qca_chain_footprint", ctypes.byref(d), self.precision, ctypes.byref(size))
         return size.value
+
+    def _schedule_next(self, js: JobState) -> None:
+        target = min(js.spec.steps, js.steps_done + self.stream_every)
+        if target > js.scheduled_to:
+            _lib.call("qca_chain_schedule", self.engine.h, js.chain, target - js.scheduled_to)
+            js.scheduled_to = target
 
     def _admit(self, now: float) -> None:
         while self.pending and self.pending[0].arrival <= now and len(self.active) < self.max_resident:
@@ -102,6 +114,12 @@ class Server:
             js.admitted = now
             self.used += need
             self.active.append(js)
+            self._schedule_next(js)
+
+    def _progress(self, js: JobState) -> tuple[int, bool, int]:
+        pr = (ctypes.c_longlong * 4)()
+        _lib.call("qca_chain_progress", self.engine.h, js.chain, pr)
+        return int(pr[0]), bool(pr[2]), int(pr[3])
 
     def _measure(self, jobs: list[JobState]) -> None:
         if not jobs:
@@ -119,44 +137,57 @@ class Server:
             if self.on_populations:
                 self._deliver(j.job_id, j.steps_done, p)
 
+    def _retire(self, js: JobState, t: float, failed: bool = False) -> None:
+        js.finished = t
+        _lib.call("qca_chain_remove", self.engine.h, js.chain)
+        self.used -= js.bytes
+        (self.failed if failed else self.done).append(js)
+
     # ------------------------------------------------------------------ loop
-    def round(self, now: float | None = None, deadline: float | None = None) -> bool:
-        """Admit what has arrived, advance the resident jobs by one step (group by
-        group, until ``deadline``), stream populations, retire finished jobs.
+    def round(self, now: float | None = None, ticks: int | None = None) -> bool:
+        """Admit what has arrived, run up to ``ticks`` lock-step ticks over the
+        resident jobs, stream the populations of jobs that reached their next
+        streaming step, schedule their next steps and retire finished jobs.
         Returns False when idle."""
         now = time.perf_counter() if now is None else now
         t_round = time.perf_counter()
         self._admit(now)
         if not self.active:
             return bool(self.pending)
-        stepped = []
-        for g0 in range(0, len(self.active), max(1, self.group)):
-            if deadline is not None and time.perf_counter() > deadline:
-                break
-            grp = self.active[g0:g0 + max(1, self.group)]
-            ids = (ctypes.c_int * len(grp))(*[j.chain for j in grp])
-            _lib.call("qca_engine_step_chains", self.engine.h, ids, len(grp), 1, None)
-            for j in grp:
-                j.steps_done += 1
-                self.site_updates += j.spec.site_updates_per_step()
-            stepped += grp
-        due = [j for j in stepped if j.steps_done % self.stream_every == 0 or j.steps_done >= j.spec.steps]
+        self.max_overlap = max(self.max_overlap, len(self.active))
+        ids = (ctypes.c_int * len(self.active))(*[j.chain for j in self.active])
+        try:
+            _lib.call("qca_engine_advance", self.engine.h, ids, len(self.active),
+                      self.ticks_per_round if ticks is None else ticks, None)
+        except _lib.QcaError as e:
+            if e.code not in (_lib.QCA_ERR_NAN, _lib.QCA_ERR_NOT_CONVERGED):
+                raise
+        due, still = [], []
+        t = time.perf_counter()
+        for j in self.active:
+            done, inside, status = self._progress(j)
+            if status:
+                j.error = f"status {status}"
+                self._retire(j, t, failed=True)
+                continue
+            if not inside and done >= j.scheduled_to and done > j.steps_done:
+                self.site_updates += (done - j.steps_done) * j.spec.site_updates_per_step()
+                j.steps_done = done
+                due.append(j)
+            still.append(j)
         self._measure(due)
         t = time.perf_counter()
-        self.round_times.append(t - t_round)
         for j in due:
             if len(j.stream) == 1:
                 self.first_stream.append(t - j.arrival)
-        still = []
-        for j in self.active:
+        self.active = []
+        for j in still:
             if j.steps_done >= j.spec.steps:
-                j.finished = t
-                _lib.call("qca_chain_remove", self.engine.h, j.chain)
-                self.used -= j.bytes
-                self.done.append(j)
+                self._retire(j, t)
             else:
-                still.append(j)
-        self.active = still
+                self._schedule_next(j)
+                self.active.append(j)
+        self.round_times.append(time.perf_counter() - t_round)
         return True
 
     # ------------------------------------------------------------------ completion thread
@@ -187,7 +218,8 @@ class Server:
             self._done_q = None
 
     def run(self, jobs: list[Job], time_limit: float | None = None) -> dict:
-        """Replay a request trace in real time (arrival offsets in seconds)."""
+        """Replay a request trace in real time (arrival offsets in seconds); with a
+        time limit, no job is admitted after it and the rounds stop there."""
         t0 = time.perf_counter()
         for job in sorted(jobs, key=lambda j: j.arrival):
             self.submit(job.spec, t0 + job.arrival)
@@ -197,9 +229,7 @@ class Server:
                 break
             if not self.active and self.pending and self.pending[0].arrival > now:
                 time.sleep(min(0.01, self.pending[0].arrival - now))
-            # no admissions that would start after the time limit
-            self.round(now if time_limit is None or now - t0 < time_limit else t0,
-                       None if time_limit is None else t0 + time_limit)
+            self.round(now)
         elapsed = time.perf_counter() - t0
         self.close()
         return self.report(elapsed)
@@ -212,7 +242,8 @@ class Server:
         def pct(a, q):
             return float(np.percentile(a, q)) if a.size else None
 
-        return {"jobs_done": len(self.done), "jobs_pending": len(self.pending), "jobs_active": len(self.active),
+        return {"jobs_done": len(self.done), "jobs_failed": len(self.failed), "jobs_pending": len(self.pending),
+                "jobs_active": len(self.active), "max_resident": self.max_overlap,
                 "site_updates": self.site_updates, "elapsed_s": elapsed,
                 "site_updates_per_s": self.site_updates / elapsed if elapsed > 0 else 0.0,
                 "p50_latency_s": pct(lat, 50), "p99_latency_s": pct(lat, 99),

@@ -184,8 +184,9 @@ def gen_measure(ref):
 
 
 def main() -> None:
-    ref_path = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    ref = load_reference(ref_path)
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the reference checkout>")
+    ref = load_reference(sys.argv[1])
     gen_mpo(ref)
     gen_exact(ref)
     gen_tdvp(ref)

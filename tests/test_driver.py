@@ -1,9 +1,11 @@
 """The driver loop (quantum_game.py:28-119) on the host, with oracle-backed
 stand-ins for the GPU algorithms: measurement cadence, the exact path's scaled
 step, file names and CSV / npz backups, several initial states in one run."""
+import os
 import types
 
 import numpy as np
+import pytest
 
 from oracle import qca_oracle as O
 from qca_gb300 import driver
@@ -47,6 +49,14 @@ class OracleTDVP(OracleExact):
         self.orc.step()
         self.v = O.mps_as_vector(self.orc.A)
 
+    def measure(self, population, d_population, single_site_entropy, bond_dims):
+        # mps.py:100-140, re-gauging the stored MPS like the reference
+        pop, dpop, sse, bonds = O.measure(self.orc.A)
+        population[:] = pop
+        d_population[:] = dpop
+        single_site_entropy[:] = sse
+        bond_dims[:] = bonds
+
 
 def make_args(algorithm):
     return types.SimpleNamespace(rules=Rules(6, range(1, 2), 1), algorithm=algorithm, step_size=0.1, num_steps=6,
@@ -88,3 +98,31 @@ def test_driver_tdvp_steps_every_step():
         assert np.abs(got - O.populations_from_vector(O.mps_as_vector(orc.A), 6)).max() < 1e-12
         orc.step()
         orc.step()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("algorithm", ["exact", "2tdvp", "1tdvp"])
+def test_driver_over_gpu_algorithms_matches_oracle_run(tmp_path, algorithm):
+    """The driver loop over GpuExact / GpuTDVP (the classes quantum_game.py:62-68
+    would select) writes the same files under the same names as the run over the
+    oracle-backed stand-ins, with the same observables: populations within 1e-8,
+    identical rounded populations and bond dimensions."""
+    args = make_args(algorithm)
+    args.precision = "fp64"
+    H = MPO.hamiltonian_from_rules(args.rules)
+    p = np.sin(O.random_thetas(6, 21)) ** 2
+    stand_in = OracleExact if algorithm == "exact" else OracleTDVP
+    gpu_dir, ref_dir = tmp_path / "gpu", tmp_path / "ref"
+    got = driver.run(args, [MPS.from_density_distribution(p)], H, out_dir=str(gpu_dir), state_names=["rand"])
+    want = driver.run(args, [MPS.from_density_distribution(p)], H, out_dir=str(ref_dir), state_names=["rand"],
+                      algorithm_cls=stand_in)
+    assert got[0]["name"] == want[0]["name"]
+    assert sorted(os.listdir(gpu_dir)) == sorted(os.listdir(ref_dir))
+    assert np.abs(got[0]["population"] - want[0]["population"]).max() < 1e-8
+    assert np.array_equal(got[0]["d_population"], want[0]["d_population"])
+    if algorithm != "exact":
+        assert np.array_equal(got[0]["bond_dims"], want[0]["bond_dims"])
+    rows = np.loadtxt(gpu_dir / f"{got[0]['name']}-population.csv", delimiter=",")
+    assert np.abs(rows - want[0]["population"]).max() < 1e-8
+    back = MPS.from_file(str(gpu_dir / f"{got[0]['name']}.npz"))
+    assert len(back.A) == 6

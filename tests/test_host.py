@@ -124,50 +124,76 @@ def test_poisson_trace_shape():
 
 
 def _fake_serving(monkeypatch):
-    """The serving module with its engine faked on the host: every engine call of a
-    step takes one second of a fake clock."""
+    """The serving module with its engine faked on the host: every tick of every
+    chain completes one local update; a chain completes a time step after
+    ``ticks_per_step`` ticks; every engine call takes one second of a fake clock."""
     from qca_gb300 import serving
     clock = {"t": 0.0}
-    stepped = []
+    chains = {}
+    calls = []
+    ticks_per_step = 3
 
     class FakeEngine:
         def __init__(self, *a, **k):
             self.h = ctypes.c_void_p(1)
 
     def fake_call(name, *args):
+        calls.append(name)
         if name == "qca_chain_footprint":
             args[2]._obj.value = 1000
         elif name == "qca_chain_add":
             fake_call.next_id += 1
             args[3]._obj.value = fake_call.next_id
-        elif name == "qca_engine_step_chains":
-            stepped.append(args[2])
-            clock["t"] += 1.0  # every engine call takes one second
+            chains[fake_call.next_id] = {"done": 0, "todo": 0, "tick": 0}
+        elif name == "qca_chain_schedule":
+            chains[args[1]]["todo"] += args[2]
+        elif name == "qca_engine_advance":
+            ids = [args[1][i] for i in range(args[2])]
+            for _ in range(args[3]):
+                for cid in ids:
+                    c = chains[cid]
+                    if c["todo"] > 0:
+                        c["tick"] += 1
+                        if c["tick"] == ticks_per_step:
+                            c["tick"] = 0
+                            c["todo"] -= 1
+                            c["done"] += 1
+            clock["t"] += 1.0
+        elif name == "qca_chain_progress":
+            c = chains[args[1]]
+            args[2][0], args[2][1], args[2][2], args[2][3] = c["done"], c["todo"], int(c["tick"] > 0), 0
+        elif name == "qca_chain_remove":
+            del chains[args[1]]
     fake_call.next_id = 0
     monkeypatch.setattr(serving, "_Engine", FakeEngine)
     monkeypatch.setattr(serving._lib, "call", fake_call)
     monkeypatch.setattr(serving.time, "perf_counter", lambda: clock["t"])
     monkeypatch.setattr(serving.time, "sleep", lambda s: clock.__setitem__("t", clock["t"] + s))
-    return serving, clock, stepped
+    return serving, clock, calls
 
 
-def test_serving_round_stops_at_its_deadline(monkeypatch):
-    """The serving loop's host logic with the engine faked: a round steps the
-    resident jobs group by group and leaves the groups after its deadline for the
-    next round; a bounded run overruns its wall time by at most one group step."""
+def test_serving_jobs_progress_at_their_own_pace(monkeypatch):
+    """The serving loop's host logic with the engine faked: every admitted job has
+    its next streaming interval scheduled, a round advances all of them by a few
+    ticks, a short job finishes and leaves while a long one keeps running, and a
+    job arriving later is admitted at the next round; a bounded run stops at its
+    time limit."""
     from qca_gb300.workloads import ChainSpec
-    serving, clock, stepped = _fake_serving(monkeypatch)
-    spec = ChainSpec(n=6, distance=1, interval=range(1, 2), chi=4, p=np.full(6, 0.5), steps=100)
-    srv = serving.Server("mixed", hbm_budget_bytes=1 << 30, stream_every=1000, max_resident=5, group=2)
-    for _ in range(5):
-        srv.submit(spec, arrival=0.0)
-    srv.round(now=0.0, deadline=0.5)  # first group runs, then the deadline has passed
-    assert stepped == [2]
-    assert [j.steps_done for j in srv.active] == [1, 1, 0, 0, 0]
-    srv.round(now=1.0)  # no deadline: every group
-    assert stepped == [2, 2, 2, 1]
-    rep = srv.run([], time_limit=2.5)  # 2 groups fit, the third starts after the limit
-    assert rep["elapsed_s"] <= 2.5 + 1.0
+    serving, clock, calls = _fake_serving(monkeypatch)
+    short = ChainSpec(n=6, distance=1, interval=range(1, 2), chi=4, p=np.full(6, 0.5), steps=2)
+    long_ = ChainSpec(n=6, distance=1, interval=range(1, 2), chi=4, p=np.full(6, 0.5), steps=100)
+    srv = serving.Server("mixed", hbm_budget_bytes=1 << 30, stream_every=4, max_resident=5, ticks_per_round=6)
+    srv.submit(short, arrival=0.0)
+    srv.submit(long_, arrival=0.0)
+    srv.submit(short, arrival=1.5)
+    srv.round(now=0.0)  # 6 ticks: the short job completes its 2 steps, the long one 2 of its first 4
+    assert [j.job_id for j in srv.done] == [0]
+    assert [j.job_id for j in srv.active] == [1] and srv.active[0].steps_done == 0
+    srv.round(now=2.0)  # the late job joins; the long job reaches step 4 and streams
+    assert [j.job_id for j in srv.done] == [0, 2]
+    assert srv.active[0].steps_done == 4 and len(srv.active[0].stream) == 1
+    rep = srv.run([], time_limit=3.5)
+    assert rep["elapsed_s"] <= 3.5 + 1.0 and rep["jobs_done"] == 2 and rep["jobs_active"] == 1
 
 
 def test_bench_roofline_arithmetic():

@@ -5,6 +5,7 @@ unitary and time-reversible exact evolution, and 2TDVP at full bond dimension
 tracking the exact evolution with its integrator's order."""
 import numpy as np
 import pytest
+from scipy.linalg import expm as scipy_expm
 
 from oracle import qca_oracle as O
 
@@ -130,3 +131,44 @@ def test_oracle_2tdvp_full_bond_tracks_exact():
         worst[dt] = w
     assert worst[0.1] < 5e-5 and worst[0.05] < 5e-6
     assert worst[0.1] / worst[0.05] > 4.0
+
+
+def test_heff_apply_is_the_transposed_assembled_matrix():
+    """The matrix-free operator equals M^T of the reference's assembled effective
+    Hamiltonian (tdvp.py:298-326 with lautils.py:80-81), for the 1-/2-site form and
+    the bond form."""
+    rng = np.random.default_rng(0)
+    Dl, Dr, wl, wr = 3, 4, 5, 6
+    cx = lambda *s: rng.standard_normal(s) + 1j * rng.standard_normal(s)  # noqa: E731
+    L, R, W, x = cx(Dl, wl, Dl), cx(Dr, wr, Dr), cx(4, 4, wl, wr), cx(4, Dl, Dr)
+    M = O._heff_site(L, R, W)
+    assert np.abs(O.heff_apply(L, R, W, x).reshape(-1) - M.T @ x.reshape(-1)).max() < 1e-12
+    Rb, xb = cx(Dr, wl, Dr), cx(Dl, Dr)
+    K = O._keff_bond(L, Rb)
+    assert np.abs(O.heff_apply(L, Rb, None, xb).reshape(-1) - K.T @ xb.reshape(-1)).max() < 1e-12
+
+
+def test_krylov_expm_matches_dense_exponential():
+    rng = np.random.default_rng(1)
+    a = rng.standard_normal((60, 60)) + 1j * rng.standard_normal((60, 60))
+    h = a + a.conj().T
+    v = rng.standard_normal(60) + 1j * rng.standard_normal(60)
+    want = scipy_expm(-1j * 0.3 * h) @ v
+    got = O.krylov_expm(lambda x: h @ x, v, 0.3)
+    assert np.abs(got - want).max() < 1e-11
+
+
+@pytest.mark.parametrize("alg", ["2tdvp", "1tdvp"])
+def test_krylov_tdvp_oracle_matches_dense_oracle(alg):
+    """The matrix-free TDVP restatement (Lanczos local exponentials) used beyond the
+    reach of the dense eigh gives the dense oracle's state and bond dimensions."""
+    n = 9
+    p = np.sin(O.random_thetas(n, 77)) ** 2
+    W = O.build_mpo(O.Rules(n, range(2, 4), 2))
+    a = O.TDVPOracle(O.mps_from_density_distribution(p), W, alg, 0.05, 12, 1e-9)
+    b = O.TDVPKrylovOracle(O.mps_from_density_distribution(p), W, alg, 0.05, 12, 1e-9)
+    for _ in range(3):
+        a.step()
+        b.step()
+        assert [x.shape for x in a.A] == [x.shape for x in b.A]
+    assert np.abs(O.mps_as_vector(a.A) - O.mps_as_vector(b.A)).max() < 1e-10

@@ -1,6 +1,6 @@
-"""Serving loop: jobs that arrive while others run are admitted between steps
-and share every launch; each job's streamed populations equal the same job run
-alone (FP64: 1e-12; mixed: 1e-6)."""
+"""Serving loop: jobs that arrive while others run are admitted between rounds
+and share every launch (the engine's lock-step ticks); each job's streamed
+populations equal the same job run alone (FP64: 1e-12; mixed: 1e-6)."""
 import numpy as np
 import pytest
 
@@ -23,19 +23,17 @@ def test_each_job_same_alone_and_in_the_mix(precision, tol):
     from qca_gb300.serving import Server
     ss = specs()
     arrivals = [0.0, 0.0, 1.5, 3.0, 3.5]  # virtual arrival times; one round per time unit
-    mix = Server(precision, hbm_budget_bytes=8 << 30, stream_every=5)
+    mix = Server(precision, hbm_budget_bytes=8 << 30, stream_every=5, ticks_per_round=8)
     for s, a in zip(ss, arrivals):
         mix.submit(s, a)
     t = 0.0
-    overlap = 0
     while mix.pending or mix.active:
         mix.round(now=t)
-        overlap = max(overlap, len(mix.active))
         t += 1.0
-    assert len(mix.done) == len(ss) and overlap >= 3
+    assert len(mix.done) == len(ss) and mix.max_overlap >= 3
     by_id = {j.job_id: j for j in mix.done}
     for k, s in enumerate(ss):
-        alone = Server(precision, hbm_budget_bytes=8 << 30, stream_every=5)
+        alone = Server(precision, hbm_budget_bytes=8 << 30, stream_every=5, ticks_per_round=5)
         alone.submit(s, 0.0)
         while alone.pending or alone.active:
             alone.round(now=1e9)
@@ -60,3 +58,25 @@ def test_admission_waits_for_memory():
         srv.round(now=1e9)
         assert srv.used <= srv.budget and len(srv.active) <= 1
     assert len(srv.done) == 3
+
+
+def test_failed_job_is_retired_and_the_others_complete():
+    """A job whose state holds a NaN fails with QCA_ERR_NAN inside a round; the
+    server retires it and the other jobs complete with their results alone."""
+    from qca_gb300.serving import Server
+    ss = specs()[:3]
+    bad = specs()[2]
+    bad.p = bad.p.copy()
+    bad.p[3] = np.nan
+    srv = Server("fp64", hbm_budget_bytes=8 << 30, stream_every=5)
+    for s in ss + [bad]:
+        srv.submit(s, 0.0)
+    while srv.pending or srv.active:
+        srv.round(now=1e9)
+    assert len(srv.done) == 3 and len(srv.failed) == 1 and srv.failed[0].job_id == 3
+    alone = Server("fp64", hbm_budget_bytes=8 << 30, stream_every=5)
+    alone.submit(ss[1], 0.0)
+    while alone.pending or alone.active:
+        alone.round(now=1e9)
+    got = {j.job_id: j for j in srv.done}[1].stream
+    assert np.abs(got[-1][1] - alone.done[0].stream[-1][1]).max() < 1e-12

@@ -71,6 +71,28 @@ def test_noalloc_matches_exact_step_twice(n, d, lo, hi):
             _lib.load().qca_exact_destroy(h)
 
 
+def test_noalloc_in_place_matches_exact_step_twice():
+    """psi_in and psi_out may be the same buffer: the state is read into the
+    scratch basis before the output is written."""
+    from qca_gb300 import _lib
+    n, d, lo, hi, m, dt = 12, 2, 2, 4, 30, 0.05
+    rng = np.random.default_rng(3)
+    psi = rng.standard_normal(1 << n) + 1j * rng.standard_normal(1 << n)
+    psi /= np.linalg.norm(psi)
+    ref = _handle(n, d, lo, hi, m)
+    buf = _handle(n, d, lo, hi, m)  # its device state is both input and output
+    try:
+        _set(ref, psi)
+        _set(buf, psi)
+        for call in range(2):
+            _lib.call("qca_exact_step", ref, dt, 2, None)
+            _lib.call("qca_exact_step_noalloc", n, d, lo, hi, m, dt, 2, _dev(buf), _dev(buf), None)
+            assert np.abs(_get(buf, n) - _get(ref, n)).max() < TOL, call
+    finally:
+        for h in (ref, buf):
+            _lib.load().qca_exact_destroy(h)
+
+
 def test_noalloc_rejects_states_beyond_its_scratch():
     from qca_gb300 import _lib
     dummy = ctypes.c_void_p(1)
