@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--chains", type=int, default=256)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--acc-chains", type=int, default=8,
+                    help="chains of the batched mix re-run in mixed and FP64 precision for the accuracy leg")
     return ap.parse_args()
 
 
@@ -345,17 +347,21 @@ def run_tdvp(args, dist: Dist):
     torch.cuda.synchronize()
     clocks.start()
     profiler_region(True)
-    e0, e1 = cuda_events()
-    e0.record()
-    _lib.call("qca_engine_step_chains", eng.h, cids, len(ids), args.steps, None)
-    e1.record()
+    ev = [cuda_events()[0] for _ in range(args.steps + 1)]
+    ev[0].record()
+    for k in range(args.steps):  # one engine call per time step: per-step latencies
+        _lib.call("qca_engine_step_chains", eng.h, cids, len(ids), 1, None)
+        ev[k + 1].record()
     torch.cuda.synchronize()
     profiler_region(False)
     clk = clocks.stop()
     dist.barrier()
-    ms = dist.max(e0.elapsed_time(e1))
+    step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    ms = dist.max(ev[0].elapsed_time(ev[args.steps]))
     ks = kernel_stats(eng)
     _lib.call("qca_engine_profile", eng.h, 0)
+    acc_idx = accuracy_subset(specs, args.acc_chains)
+    acc_pops = measure_pops(eng, [ids[i] for i in acc_idx], [specs[i] for i in acc_idx]) if acc_idx else None
     total_su = dist.sum(su_per_step * args.steps)
     value = total_su / (ms / 1e3)
     bonds = []
@@ -372,6 +378,9 @@ def run_tdvp(args, dist: Dist):
     if not args.no_e2e:
         e2e = run_e2e(args, specs, [get_mps(eng, cid, s.n) for cid, s in zip(ids, specs)], prec, dist)
     del eng
+    acc = None
+    if acc_idx:
+        acc = accuracy_leg(args, [specs[i] for i in acc_idx], acc_pops, value)
     cpu = None
     if not args.no_cpu and dist.rank == 0:
         v, sample = cpu_tdvp_sample(specs, 15.0)
@@ -386,8 +395,70 @@ def run_tdvp(args, dist: Dist):
                    "site_updates_per_step": su_per_step, "max_bond_dim_reached": max(bonds),
                    "l2": "working set larger than L2 (>= %.1f GB resident)" % (len(specs) * 0.01)},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+        "step_latency_ms": {"p50": round(float(np.percentile(step_ms, 50)), 2),
+                            "p99": round(float(np.percentile(step_ms, 99)), 2)},
+        "accuracy": acc,
     }
+    if acc is not None:
+        line["fp64"] = acc.pop("fp64")
     return line
+
+
+def accuracy_subset(specs, count: int) -> list[int]:
+    """Every (len/count)-th chain of the workload: a sample of its mix of lengths,
+    rules and bond caps."""
+    if count <= 0:
+        return []
+    stride = max(1, len(specs) // count)
+    return list(range(0, len(specs), stride))[:count]
+
+
+def measure_pops(eng, ids, specs) -> np.ndarray:
+    from qca_gb300 import _lib
+    n_tot = sum(s.n for s in specs)
+    pop = np.zeros(n_tot)
+    cids = (ctypes.c_int * len(ids))(*ids)
+    _lib.call("qca_engine_measure", eng.h, cids, len(ids), pop.ctypes.data_as(_lib._PD), None, None, None, None)
+    return pop
+
+
+def accuracy_leg(args, specs, pops_batched, batched_value: float) -> dict:
+    """The metric's accuracy condition and its FP64 leg on a sample of the timed
+    chains: the same chains from the same product states through the same
+    warm-up + timed steps, (a) with the mixed path alone (its populations are
+    compared with the batched run's) and (b) with the plain FP64 path, <n_i>
+    compared after every step; the FP64 path's site-updates/s over the timed
+    steps is the metric's plain-FP64 rate."""
+    import torch
+    from qca_gb300 import _lib
+    from qca_gb300.algorithms import _Engine
+    series, rates = {}, {}
+    total = args.warmup + args.steps
+    for name, prec in (("mixed", _lib.QCA_PREC_MIXED), ("fp64", _lib.QCA_PREC_FP64)):
+        eng = _Engine(prec)
+        ids = add_chains(eng, specs, prec)
+        cids = (ctypes.c_int * len(ids))(*ids)
+        rows, t_timed = [], 0.0
+        for step in range(total):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            _lib.call("qca_engine_step_chains", eng.h, cids, len(ids), 1, None)
+            torch.cuda.synchronize()
+            if step >= args.warmup:
+                t_timed += time.perf_counter() - t0
+            rows.append(measure_pops(eng, ids, specs))
+        series[name] = np.array(rows)
+        rates[name] = sum(s.site_updates_per_step() for s in specs) * args.steps / t_timed
+        del eng
+    dn = np.abs(series["mixed"] - series["fp64"]).max(axis=1)
+    return {"max_dn_vs_fp64": float(dn.max()), "max_dn_by_step": [float(f"{x:.3g}") for x in dn],
+            "steps": total, "chains": len(specs),
+            "chains_desc": [(s.n, s.distance, s.interval.stop - 1, s.chi) for s in specs],
+            "batched_vs_alone_max_dn": float(np.abs(series["mixed"][-1] - pops_batched).max()),
+            "fp64": {"site_updates_per_s": round(rates["fp64"], 2),
+                     "measured_on": f"the {len(specs)} sampled chains, steps {args.warmup}..{total - 1}",
+                     "mixed_same_chains_site_updates_per_s": round(rates["mixed"], 2),
+                     "batched_mixed_over_fp64": round(batched_value / rates["fp64"], 2)}}
 
 
 def run_e2e(args, specs, states, prec, dist: Dist):

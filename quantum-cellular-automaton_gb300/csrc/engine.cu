@@ -152,6 +152,7 @@ struct Chain {
   void* mem = nullptr;
   size_t bytes = 0;
   int max_chunks = 1;
+  int cmax = 1;  // largest bond capacity
   // sweep state
   int dir = 0;  // 0 right, 1 left
   int pos = 0;
@@ -494,7 +495,9 @@ struct Engine final : EngineBase {
     const std::vector<Span> sp = spans();
     for (auto& d : q) {
       const int K = std::min(d.m, d.n), qc = d.complete ? d.m : K;
-      const long long ein = ext(d.rsplit, d.sIr0) + ext((d.m + d.rsplit - 1) / d.rsplit, d.sIr1) + ext(d.n, d.sIc);
+      const long long ein = ext(d.rsplit, d.sIr0) + ext((d.m + d.rsplit - 1) / d.rsplit, d.sIr1) +
+                            (d.csplit > 0 ? ext(d.csplit, d.sIc) + ext((d.n + d.csplit - 1) / d.csplit, d.sIc1)
+                                          : ext(d.n, d.sIc));
       if (!in_spans<T>(sp, d.in, ein)) return bad("qr in");
       if (!in_spans<T>(sp, d.work, (long long)d.m * d.n + (long long)d.m * qc - 1)) return bad("qr work");
       if (!in_spans<T>(sp, d.tau, K - 1)) return bad("qr tau");
@@ -509,12 +512,15 @@ struct Engine final : EngineBase {
   int check_svd(const std::vector<SvdDesc<T>>& v) const {
     const std::vector<Span> sp = spans();
     for (auto& d : v) {
-      const long long m = 2LL * d.Dl, n = 2LL * d.Dr, nx = std::min(m, n), mx = std::max(m, n);
+      const long long p = d.right_sweep ? 2LL * d.Dl : 2LL * d.Dr, q = d.right_sweep ? 2LL * d.Dr : 2LL * d.Dl;
+      const long long K = std::min(p, q);
       if (!in_spans<T>(sp, d.theta, 4LL * d.Dl * d.Dr - 1)) return bad("svd theta");
-      if (!in_spans<T>(sp, d.work, mx * nx + nx * nx - 1)) return bad("svd work");
+      if (!in_spans<T>(sp, d.work, K * K - 1)) return bad("svd work");
+      if (!in_spans<T>(sp, d.qmat, p * K - 1)) return bad("svd Q");
+      if (!in_spans<T>(sp, d.rmat, K * q - 1)) return bad("svd R");
       if (!in_spans<T>(sp, d.Al, 2LL * d.Dl * d.kmax - 1)) return bad("svd Al");
       if (!in_spans<T>(sp, d.Ar, 2LL * d.kmax * d.Dr - 1)) return bad("svd Ar");
-      if (nx > 1024) return bad("svd size");
+      if (K > 1024) return bad("svd size");
     }
     return QCA_OK;
   }
@@ -1095,7 +1101,7 @@ struct Engine final : EngineBase {
     QCA_TRY(lanczos(P, st));
     // stage 2: split (SVD) / complete QR
     std::vector<SvdDesc<T>> sv;
-    std::vector<QrDesc<T>> qr;
+    std::vector<QrDesc<T>> qr, spre;
     std::vector<Chain<T>*> svc;
     for (auto* c : C) {
       if (c->algo == QCA_ALGO_2TDVP) {
@@ -1111,7 +1117,14 @@ struct Engine final : EngineBase {
         d.right_sweep = c->dir == 0;
         d.Al = c->alt(l);
         d.Ar = c->alt(r);
-        d.work = c->svdw;
+        // workspace: Q (p K <= 4 cmax^2), R (K q), V (K^2); the QR's own work in qrw
+        const long long c2 = 4LL * c->cmax * c->cmax;
+        cplx<T>* qbuf = c->svdw;
+        cplx<T>* rbuf = c->svdw + c2;
+        d.qmat = qbuf;
+        d.rmat = rbuf;
+        d.work = c->svdw + 2 * c2;
+        spre.push_back(split_qr_desc<T>(c->theta, d.Dl, d.Dr, d.right_sweep, c->qrw, c->qrtau, qbuf, rbuf));
         d.sv = c->sv;
         d.k_out = c->iflags;
         d.discarded = c->dscal;
@@ -1179,6 +1192,12 @@ struct Engine final : EngineBase {
     }
     if (!sv.empty()) {
       QCA_TRY(check_svd(sv));
+      QCA_TRY(check_qr(spre));
+      {  // the preconditioning QRs of the splits (FP32 sums on the mixed path)
+        const QrDesc<T>* dq;
+        QCA_TRY(upload(spre, st, &dq));
+        QCA_TRY(timed(KC_SVD, 0, 0, st, [&] { return launch_qr<T>(dq, (int)spre.size(), 1, st); }));
+      }
       double fl = 0.0;
       for (auto& d : sv) {  // Golub-Van Loan thin-SVD count, x4 for complex
         const double m = 2.0 * std::max(d.Dl, d.Dr), n = 2.0 * std::min(d.Dl, d.Dr);
@@ -1856,7 +1875,7 @@ static void plan_chain(const qca_chain_desc* d, int mmax, Layout& Lo, std::vecto
   put(es * nmax * (mmax + 1));              // basis
   put(es * tmax);                           // t1
   put(es * tmax);                           // t2
-  put(es * 8ull * cmax * cmax);             // svd work (mx*nx + nx*nx, nx <= mx <= 2 cmax)
+  put(es * 12ull * cmax * cmax);            // svd work: Q (p K), R (K q), V (K^2); p, q, K <= 2 cmax
   put(es * (8ull * cmax * cmax + 2 * cmax));  // qr work (m*n + m*m), m <= 2 cmax, n <= 2 cmax
   put(es * 2 * cmax);                       // qr tau
   put(es * (size_t)cmax * cmax * 2);        // cbuf
@@ -1952,6 +1971,7 @@ int Engine<T>::add(const qca_chain_desc* d, cudaStream_t st, int* id_out) {
   }
   c->nmax = nmax;
   c->max_chunks = chunks;
+  c->cmax = cmax;
   size_t k = 0;
   c->A[0].resize(N);
   c->A[1].resize(N);

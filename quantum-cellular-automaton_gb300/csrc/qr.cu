@@ -40,9 +40,12 @@ __global__ void __launch_bounds__(kQrThreads) qr_kernel(const QrDesc<T>* __restr
   cplx<T>* A = D.work;                       // column-major m x n
   cplx<T>* Q = D.work + (long long)m * n;    // column-major m x qc
   const int qc = D.complete ? m : K;
+  const int csplit = D.csplit > 0 ? D.csplit : n;
   for (long long e = threadIdx.x; e < (long long)m * n; e += blockDim.x) {
     const int c = (int)(e / m), r = (int)(e - (long long)c * m);
-    A[e] = D.in[(r / D.rsplit) * D.sIr1 + (r % D.rsplit) * D.sIr0 + c * D.sIc];
+    cplx<T> v = D.in[(r / D.rsplit) * D.sIr1 + (r % D.rsplit) * D.sIr0 + (c / csplit) * D.sIc1 + (c % csplit) * D.sIc];
+    if (D.conj_in) v.im = -v.im;
+    A[e] = v;
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;

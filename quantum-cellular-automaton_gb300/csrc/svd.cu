@@ -3,15 +3,20 @@
 //   k = min{ i : ||s[i:]||_2 < eps }  capped at min(chi, len s)
 // and s renormalised (lautils.normalize, lautils.py:4-5).
 //
-// One-sided (Hestenes) Jacobi on the narrower orientation W (mx >= nx):
-// W = Theta when 2 Dr <= 2 Dl, else W = Theta^H, with the rotations accumulated
-// into V (nx x nx).  At convergence X = W V has orthogonal columns whose FP64
-// norms are the singular values; the site tensors are written directly from X
-// and V:
-//   W = Theta:    U = X / sigma,  Vh = V^H
-//   W = Theta^H:  U = V,          Vh = (X / sigma)^H
-// with the renormalised singular values multiplied into A_r (right sweep) or
-// A_l (left sweep), tdvp.py:121-122 and 141-142.
+// QR-preconditioned one-sided (Hestenes) Jacobi.  The matrix W = Theta on a right
+// sweep (the left factor must come out an isometry) or W = Theta^H on a left
+// sweep (the right factor must) is first factored W = Q R by Householder
+// reflections (qr.cu, launched before these kernels), and the Jacobi rotations
+// run on X = R^H (q x K) with the rotations accumulated into V (K x K).  The
+// two-site matrices of TDVP have exponentially graded spectra; on them Jacobi
+// applied to W directly converges linearly and needs dozens of sweeps, while on
+// R^H, whose columns are already nearly orthogonal and graded, a handful suffice.
+// At convergence W = (Q V) Sigma (X / Sigma)^H with X = R^H V, so the site tensors
+// are written from
+//   the isometric factor Q V (column j: Q times V column j, FP32 or FP64 sums),
+//   the other factor X itself (it carries the singular values),
+// with the renormalised singular values in the non-isometric factor (tdvp.py:
+// 121-122 and 141-142).  The singular values are the FP64 norms of X's columns.
 //
 // Two kernels over a thread-block cluster (1..16 CTAs, distributed shared memory):
 //  * svd_block_kernel (column length <= 256): the columns form 2P blocks of at most
@@ -218,22 +223,27 @@ __device__ __forceinline__ bool jacobi_rotate(cplx<T> (&xu)[RPL], cplx<T> (&xv)[
   return true;
 }
 
-// W column col (mx rows) into dst, by the whole CTA
+// X column col (mx rows) into dst, by the whole CTA
 template <typename T>
-__device__ __forceinline__ void load_w_column(const SvdDesc<T>& D, bool trans, int mx, int nx, int col, cplx<T>* dst) {
-  const int Dl = D.Dl, Dr = D.Dr;
-  const long long blk = (long long)Dl * Dr;
+__device__ __forceinline__ void load_x_column(const SvdDesc<T>& D, int mx, int nx, int col, cplx<T>* dst) {
+  // column col of X = R^H: X[i][col] = conj(R[col][i]), R row major K x q (q = mx)
   for (int row = threadIdx.x; row < mx; row += blockDim.x) {
     cplx<T> v = mk<T>(0, 0);
     if (col < nx) {
-      const int r = trans ? col : row;
-      const int c = trans ? row : col;
-      const int s1 = r / Dl, a = r - s1 * Dl, s2 = c / Dr, cc = c - s2 * Dr;
-      v = D.theta[(long long)(s1 * 2 + s2) * blk + (long long)a * Dr + cc];
-      if (trans) v.im = -v.im;
+      v = D.rmat[(long long)col * mx + row];
+      v.im = -v.im;
     }
     dst[row] = v;
   }
+}
+
+// Shape of the preconditioned problem: W (p x q) is Theta on a right sweep and
+// Theta^H on a left sweep; Jacobi runs on X = R^H, mx = q rows and nx = K columns.
+template <typename T>
+__device__ __forceinline__ void split_shape(const SvdDesc<T>& D, int& p, int& mx, int& nx) {
+  p = D.right_sweep ? 2 * D.Dl : 2 * D.Dr;
+  mx = D.right_sweep ? 2 * D.Dr : 2 * D.Dl;
+  nx = p < mx ? p : mx;
 }
 
 // After convergence: FP64 norms of the columns (singular values), rank sort in CTA 0,
@@ -242,8 +252,8 @@ __device__ __forceinline__ void load_w_column(const SvdDesc<T>& D, bool trans, i
 // columns.  Ends with a cluster barrier: CTA 0's shared memory is read through
 // distributed shared memory until then.
 template <typename T, typename Loc>
-__device__ void svd_finish(const SvdDesc<T>& D, cg::cluster_group& cluster, int rank, const Loc& L, int mx, int nx,
-                           bool trans, int sweep, T floor2, double* snorm, int* perm, int* s_k, double* s_keep) {
+__device__ void svd_finish(const SvdDesc<T>& D, cg::cluster_group& cluster, int rank, const Loc& L, int p, int mx,
+                           int nx, int sweep, T floor2, double* snorm, int* perm, int* s_k, double* s_keep) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int Dr = D.Dr;
   double* snorm0 = cluster.map_shared_rank(snorm, 0);
@@ -317,39 +327,37 @@ __device__ void svd_finish(const SvdDesc<T>& D, cg::cluster_group& cluster, int 
   const double keep = *cluster.map_shared_rank(s_keep, 0);
   const int* perm0 = cluster.map_shared_rank(perm, 0);
   const double* sn0 = cluster.map_shared_rank(snorm, 0);
+  // Kept column i (global column j = perm[i]): the isometric factor Q v_j (p rows,
+  // Q column major p x K) and the other factor x_j / ||s_kept|| (mx = q rows).
+  //   right sweep (W = Theta):   A_l[(s1,a)][i] = (Q v_j)[(s1,a)],
+  //                              A_r[s2][i][c] = conj(x_j[(s2,c)]) / keep
+  //   left sweep  (W = Theta^H): A_l[(s1,a)][i] = x_j[(s1,a)] / keep,
+  //                              A_r[s2][i][c] = conj((Q v_j)[(s2,c)])
+  const double inv_keep = keep > 0 ? 1.0 / keep : 0.0;
   for (int i = 0; i < k; ++i) {
     const int j = perm0[i];
     if (!L.own(j)) continue;
     const cplx<T>* x = L.x(j);
     const cplx<T>* v = L.v(j);
-    const double sig = sn0[j];
-    const double inv = sig > 0 ? 1.0 / sig : 0.0;
-    const double sn = keep > 0 ? sig / keep : 0.0;  // renormalised singular value
-    const double fl = D.right_sweep ? 1.0 : sn;     // scale of A_l
-    const double fr = D.right_sweep ? sn : 1.0;     // scale of A_r
-    if (!trans) {
-      // U[:, i] = x / sigma over the m = mx rows (row = s1 * Dl + a); Vh[i, c] = conj(v[c])
-      for (int row = threadIdx.x; row < mx; row += blockDim.x) {
-        const cplx<T> u = x[row];
-        const double f = inv * fl;
-        D.Al[(long long)row * k + i] = mk<T>((T)(u.re * f), (T)(u.im * f));
+    for (int row = threadIdx.x; row < p; row += blockDim.x) {
+      cplx<T> u = mk<T>(0, 0);
+      const cplx<T>* qr = D.qmat + row;
+      for (int t = 0; t < nx; ++t) cfma(u, qr[(long long)t * p], v[t]);
+      if (D.right_sweep) {
+        D.Al[(long long)row * k + i] = u;
+      } else {
+        const int s2 = row / Dr, cc = row - s2 * Dr;
+        D.Ar[((long long)s2 * k + i) * Dr + cc] = conj(u);
       }
-      for (int c = threadIdx.x; c < nx; c += blockDim.x) {
-        const cplx<T> u = v[c];
-        const int s2 = c / Dr, cc = c - s2 * Dr;
-        D.Ar[((long long)s2 * k + i) * Dr + cc] = mk<T>((T)(u.re * fr), (T)(-u.im * fr));
-      }
-    } else {
-      // U[:, i] = v over the m = nx rows; Vh[i, c] = conj(x[c]) / sigma over the n = mx columns
-      for (int row = threadIdx.x; row < nx; row += blockDim.x) {
-        const cplx<T> u = v[row];
-        D.Al[(long long)row * k + i] = mk<T>((T)(u.re * fl), (T)(u.im * fl));
-      }
-      for (int c = threadIdx.x; c < mx; c += blockDim.x) {
-        const cplx<T> u = x[c];
-        const double f = inv * fr;
-        const int s2 = c / Dr, cc = c - s2 * Dr;
-        D.Ar[((long long)s2 * k + i) * Dr + cc] = mk<T>((T)(u.re * f), (T)(-u.im * f));
+    }
+    for (int row = threadIdx.x; row < mx; row += blockDim.x) {
+      const cplx<T> u = x[row];
+      const cplx<T> w = mk<T>((T)(u.re * inv_keep), (T)(u.im * inv_keep));
+      if (D.right_sweep) {
+        const int s2 = row / Dr, cc = row - s2 * Dr;
+        D.Ar[((long long)s2 * k + i) * Dr + cc] = conj(w);
+      } else {
+        D.Al[(long long)row * k + i] = w;
       }
     }
   }
@@ -399,10 +407,8 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
   __shared__ double s_keep;
   __shared__ double s_fro;  // ||Theta||_F^2 (CTA 0)
   __shared__ double red[33];
-  const int m = 2 * D.Dl, n = 2 * D.Dr;
-  const bool trans = n > m;
-  const int mx = trans ? n : m;
-  const int nx = trans ? m : n;
+  int p, mx, nx;
+  split_shape(D, p, mx, nx);
   // V columns: after X in shared memory, or slot-major in the global workspace
   cplx<T>* Vloc = v_smem ? Xloc + (long long)cpc * mx : D.work + (long long)rank * cpc * nx;
   for (int lc = 0; lc < cpc; ++lc) {
@@ -410,7 +416,7 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
     if (col >= nx) break;
     for (int row = threadIdx.x; row < nx; row += blockDim.x)
       Vloc[(long long)lc * nx + row] = mk<T>(row == col ? (T)1 : (T)0, (T)0);
-    load_w_column(D, trans, mx, nx, col, Xloc + (long long)lc * mx);
+    load_x_column(D, mx, nx, col, Xloc + (long long)lc * mx);
   }
   if (threadIdx.x < 2) s_flag[threadIdx.x] = 0;
   if (threadIdx.x == 0) s_fro = 0.0;
@@ -487,7 +493,7 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
     if (!any) break;
   }
   const SlabLoc<T> L{Xloc, Vloc, cpc, mx, nx, rank};
-  svd_finish<T>(D, cluster, rank, L, mx, nx, trans, sweep, floor2, snorm, perm, &s_k, &s_keep);
+  svd_finish<T>(D, cluster, rank, L, p, mx, nx, sweep, floor2, snorm, perm, &s_k, &s_keep);
 }
 
 template <typename T, int RPL>
@@ -504,10 +510,8 @@ __global__ void __launch_bounds__(kSvdThreads) svd_block_kernel(const SvdDesc<T>
   __shared__ double s_keep;
   __shared__ double s_fro;  // ||Theta||_F^2 (CTA 0)
   __shared__ double red[33];
-  const int m = 2 * D.Dl, n = 2 * D.Dr;
-  const bool trans = n > m;
-  const int mx = trans ? n : m;
-  const int nx = trans ? m : n;
+  int p, mx, nx;
+  split_shape(D, p, mx, nx);
   const int n2 = 2 * P;                // blocks (tournament players)
   const int b = (nx + n2 - 1) / n2;    // columns per block (<= kSvdBlk)
   // slots [generation][top/bottom][b columns]: X (mx each), then V (nx each) when it
@@ -525,7 +529,7 @@ __global__ void __launch_bounds__(kSvdThreads) svd_block_kernel(const SvdDesc<T>
     const int be = s == 0 ? rank : n2 - 1 - rank;
     for (int j = 0; j < b; ++j) {
       const int col = be * b + j;
-      load_w_column(D, trans, mx, nx, col, xs(0, s, j));
+      load_x_column(D, mx, nx, col, xs(0, s, j));
       if (col < nx || v_smem) {
         cplx<T>* v = vc(0, s, j, col);
         for (int row = threadIdx.x; row < nx; row += blockDim.x)
@@ -663,7 +667,7 @@ __global__ void __launch_bounds__(kSvdThreads) svd_block_kernel(const SvdDesc<T>
   }
   // after a whole sweep (2P - 1 moves) every block is back at its starting position
   const BlockLoc<T> L{xs(gen, 0, 0), v_smem ? vc(gen, 0, 0, 0) : nullptr, Vg, P, b, mx, nx, rank};
-  svd_finish<T>(D, cluster, rank, L, mx, nx, trans, sweep, floor2, snorm, perm, &s_k, &s_keep);
+  svd_finish<T>(D, cluster, rank, L, p, mx, nx, sweep, floor2, snorm, perm, &s_k, &s_keep);
 }
 
 // block kernel geometry: P CTAs (power of two, P * 32 >= nx where possible), blocks of
@@ -837,40 +841,56 @@ template <typename T>
 static int test_svd(int Dl, int Dr, const void* theta, int chi, double eps, int max_sweeps, void* Al, void* Ar,
                     double* sv, int* k_out, cudaStream_t st) {
   using namespace qca;
-  const int m = 2 * Dl, n = 2 * Dr, mx = std::max(m, n), nx = std::min(m, n);
+  const int p = 2 * Dl, q = 2 * Dr, K = std::min(p, q);
+  const size_t es = sizeof(cplx<T>);
+  // scratch: QR work (p q + p K), tau (K), Q (p K), R (K q), V (K^2), flags, descriptors
+  const size_t n_work = (size_t)p * q + (size_t)p * K, n_tau = K, n_q = (size_t)p * K, n_r = (size_t)K * q,
+               n_v = (size_t)K * K;
+  const size_t elems = n_work + n_tau + n_q + n_r + n_v;
+  const size_t fbytes = 64, dbytes = 2 * ((sizeof(SvdDesc<T>) + 63) / 64) * 64 + 2 * ((sizeof(QrDesc<T>) + 63) / 64) * 64;
   void* scratch = nullptr;
-  const size_t wbytes = sizeof(cplx<T>) * ((size_t)mx * nx + (size_t)nx * nx);
-  const size_t bytes = wbytes + 64 + sizeof(SvdDesc<T>);
-  QCA_CUDA(cudaMalloc(&scratch, bytes));
-  char* base = (char*)scratch;
+  QCA_CUDA(cudaMalloc(&scratch, elems * es + fbytes + dbytes));
+  cplx<T>* base = (cplx<T>*)scratch;
+  cplx<T>* work = base;
+  cplx<T>* tau = work + n_work;
+  cplx<T>* Q = tau + n_tau;
+  cplx<T>* R = Q + n_q;
+  cplx<T>* Vw = R + n_r;
+  char* flags = (char*)(base + elems);
+  SvdDesc<T>* dd = (SvdDesc<T>*)(flags + fbytes);
+  QrDesc<T>* dq = (QrDesc<T>*)((char*)dd + ((sizeof(SvdDesc<T>) + 63) / 64) * 64);
+  const QrDesc<T> qd = split_qr_desc<T>((const cplx<T>*)theta, Dl, Dr, 1, work, tau, Q, R);
   SvdDesc<T> d;
   memset(&d, 0, sizeof(d));
   d.theta = (const cplx<T>*)theta;
   d.Dl = Dl;
   d.Dr = Dr;
   d.chi = chi;
-  d.kmax = nx;
+  d.kmax = K;
   d.eps = eps;
   d.right_sweep = 1;
   d.max_sweeps = max_sweeps;
   d.Al = (cplx<T>*)Al;
   d.Ar = (cplx<T>*)Ar;
-  d.work = (cplx<T>*)base;
+  d.qmat = Q;
+  d.rmat = R;
+  d.work = Vw;
   d.sv = sv;
-  d.k_out = (int*)(base + wbytes);
-  d.status = (int*)(base + wbytes + 16);
-  d.discarded = (double*)(base + wbytes + 32);
-  SvdDesc<T>* dd = (SvdDesc<T>*)(base + wbytes + 64);
+  d.k_out = (int*)flags;
+  d.status = (int*)(flags + 16);
+  d.discarded = (double*)(flags + 32);
   int s = QCA_OK;
   int h[3] = {0, 0, 0};
-  if (cudaMemsetAsync(base + wbytes, 0, 64, st) != cudaSuccess ||
-      cudaMemcpyAsync(dd, &d, sizeof(d), cudaMemcpyHostToDevice, st) != cudaSuccess) {
+  if (cudaMemsetAsync(flags, 0, fbytes, st) != cudaSuccess ||
+      cudaMemcpyAsync(dd, &d, sizeof(d), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync(dq, &qd, sizeof(qd), cudaMemcpyHostToDevice, st) != cudaSuccess) {
     set_error("qca_test_svd: %s", cudaGetErrorString(cudaGetLastError()));
     s = QCA_ERR_CUDA;
   }
+  if (s == QCA_OK) s = launch_qr<T>(dq, 1, sizeof(T) == 4 ? 1 : 0, st);
   if (s == QCA_OK) s = launch_svd<T>(dd, &d, 1, st);
-  if (s == QCA_OK && (cudaMemcpyAsync(h, base + wbytes, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-                      cudaMemcpyAsync(h + 1, base + wbytes + 16, 2 * sizeof(int), cudaMemcpyDeviceToHost, st) !=
+  if (s == QCA_OK && (cudaMemcpyAsync(h, flags, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                      cudaMemcpyAsync(h + 1, flags + 16, 2 * sizeof(int), cudaMemcpyDeviceToHost, st) !=
                           cudaSuccess ||
                       cudaStreamSynchronize(st) != cudaSuccess)) {
     set_error("qca_test_svd: %s", cudaGetErrorString(cudaGetLastError()));

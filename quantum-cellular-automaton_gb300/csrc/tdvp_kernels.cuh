@@ -136,6 +136,15 @@ int launch_lz_combine(const LanczosDesc<T>* d, const LanczosDesc<T>* h, int nd, 
 // ----------------------------------------------------------------------------------
 // SVD of the two-site matrix by one-sided Jacobi + truncation (tdvp.py:286-296)
 // ----------------------------------------------------------------------------------
+// The split is preconditioned by a Householder QR (launch_qr, run first): the
+// matrix W = Theta (right sweep) or Theta^H (left sweep), p x q with
+// Theta[(s1,a),(s2,c)] = theta[s1*2+s2][a][c], is factored W = Q R (Q p x K, K =
+// min(p, q)), and one-sided Jacobi runs on X = R^H (q x K), whose columns are
+// graded and nearly orthogonal, so the sweeps converge in a few rounds instead of
+// the dozens the raw, strongly graded two-site matrix needs.  With X V
+// orthogonal: W = (Q V) Sigma (X V / Sigma)^H, so the isometric factor of the
+// split is Q V (orthonormal to rounding, whatever the singular value) and the
+// other factor is X V itself, which carries Sigma.
 template <typename T>
 struct SvdDesc {
   const cplx<T>* theta;  // theta[s][a][c], s = s1*2+s2, dims (4, Dl, Dr)
@@ -146,7 +155,9 @@ struct SvdDesc {
   int right_sweep;       // 1: A_l = U, A_r = s Vh ; 0: A_l = U s, A_r = Vh
   cplx<T>* Al;           // out (2, Dl, k)
   cplx<T>* Ar;           // out (2, k, Dr)
-  cplx<T>* work;         // V columns when they do not fit in the cluster's shared memory (n_x^2)
+  const cplx<T>* qmat;   // Q of W = Q R, column major p x K (p = 2 Dl right, 2 Dr left)
+  const cplx<T>* rmat;   // R, row major K x q (q = 2 Dr right, 2 Dl left)
+  cplx<T>* work;         // V columns when they do not fit in the cluster's shared memory (K^2)
   double* sv;            // singular values (n_x), FP64
   int* k_out;            // new bond dimension
   double* discarded;     // discarded weight accumulator (+= sum of dropped s^2 / sum s^2)
@@ -167,10 +178,15 @@ int svd_cluster_size(int Dl, int Dr);
 // ----------------------------------------------------------------------------------
 template <typename T>
 struct QrDesc {
-  // row r of the input / of Q splits as r = r1 * rsplit + r0
+  // row r of the input / of Q splits as r = r1 * rsplit + r0; column c of the input
+  // as c = c1 * csplit + c0 (csplit 0: no split), element at
+  // in[r1 sIr1 + r0 sIr0 + c1 sIc1 + c0 sIc], conjugated when conj_in
   const cplx<T>* in;
   int rsplit;
   long long sIr0, sIr1, sIc;
+  int csplit;
+  long long sIc1;
+  int conj_in;
   int m, n;
   int complete;          // 1: Q is m x m, R is m x n; 0: Q is m x K, R is K x n (K = min(m,n))
   cplx<T>* work;         // m*n (factored matrix) + m*m (Q)
@@ -190,6 +206,53 @@ struct QrDesc {
 template <typename T>
 // gauge != 0: a gauge move of the mixed path (FP32 sums); 0: FP64 sums
 int launch_qr(const QrDesc<T>* d, int nd, int gauge, cudaStream_t st);
+
+// The QR that preconditions a two-site split (see SvdDesc): W = Theta (right
+// sweep, p = 2 Dl, q = 2 Dr) or Theta^H (left sweep, p = 2 Dr, q = 2 Dl) read
+// straight from theta[s1*2+s2][a][c]; Q into q_out (column major p x K), R into
+// r_out (row major K x q).  work needs p q + p K elements, tau K.
+template <typename T>
+QrDesc<T> split_qr_desc(const cplx<T>* theta, int Dl, int Dr, int right_sweep, cplx<T>* work, cplx<T>* tau,
+                        cplx<T>* q_out, cplx<T>* r_out) {
+  QrDesc<T> d;
+  memset(&d, 0, sizeof(d));
+  const long long blk = (long long)Dl * Dr;
+  const int p = right_sweep ? 2 * Dl : 2 * Dr, q = right_sweep ? 2 * Dr : 2 * Dl, K = p < q ? p : q;
+  d.in = theta;
+  if (right_sweep) {  // rows (s1, a), columns (s2, c)
+    d.rsplit = Dl;
+    d.sIr1 = 2 * blk;
+    d.sIr0 = Dr;
+    d.csplit = Dr;
+    d.sIc1 = blk;
+    d.sIc = 1;
+  } else {  // rows (s2, c), columns (s1, a), conjugated
+    d.rsplit = Dr;
+    d.sIr1 = blk;
+    d.sIr0 = 1;
+    d.csplit = Dl;
+    d.sIc1 = 2 * blk;
+    d.sIc = Dr;
+    d.conj_in = 1;
+  }
+  d.m = p;
+  d.n = q;
+  d.complete = 0;
+  d.work = work;
+  d.tau = tau;
+  d.q = q_out;
+  d.qsplit = p;
+  d.sQr0 = 1;
+  d.sQc = p;
+  d.qrows_out = p;
+  d.qcols_out = K;
+  d.rr = r_out;
+  d.sRr = q;
+  d.sRc = 1;
+  d.rrows_out = K;
+  d.rcols_out = q;
+  return d;
+}
 
 // ----------------------------------------------------------------------------------
 // elementwise helpers
