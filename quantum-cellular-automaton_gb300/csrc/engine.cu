@@ -545,7 +545,7 @@ struct Engine final : EngineBase {
   int svd_grouped(std::vector<SvdDesc<T>>& sv, cudaStream_t st) {
     std::vector<SvdDesc<T>> grp[5];
     for (auto& d : sv) {
-      const int cs = svd_cluster_size<T>(d.Dl, d.Dr);
+      const int cs = svd_cluster_size<T>(d.Dl, d.Dr, d.right_sweep);
       const int gi = cs <= 1 ? 0 : cs == 2 ? 1 : cs == 4 ? 2 : cs == 8 ? 3 : 4;
       grp[gi].push_back(d);
     }

@@ -7,7 +7,8 @@
 //
 // H = sum_i X_i Pi_i: (H v)[x] = sum_b c_b(x) v[x ^ (1 << b)], where bit b is
 // cell N-1-b and c_b(x) = [popc(x & nmask_b) in [lo, hi)] (the flip condition of
-// tensor_networks/mpo.py:54-200, evaluated from the index alone).
+// tensor_networks/mpo.py:54-200, evaluated from the index alone; for distances up
+// to 3 for all bits at once by a bit-sliced neighbour count, flip_mask).
 //
 // One H application is split by bit groups so that every partner of an amplitude
 // lies in the same shared-memory tile:
@@ -46,7 +47,41 @@ struct ExactParams {
   int rule_lo, rule_hi;        // flip iff count in [rule_lo, rule_hi)
   uint32_t nmask[kMaxCells];   // neighbour mask of the cell at bit b
   long long dim;               // 2^n
+  int dist;                    // rule distance (flip_mask covers distance <= 3)
 };
+
+// Bits of x whose cell may flip, for all cells at once: the alive-neighbour count
+// of every bit position is accumulated bit-sliced (three planes c0, c1, c2) from
+// the index shifted by 1..dist in both directions (bits shifted past either end of
+// the chain are dead cells), and the interval test [lo, hi) becomes a few logic
+// operations on the planes.  Equivalent to popc(x & nmask_b) in [lo, hi) for
+// every b; replaces a popcount and two comparisons per bit and amplitude.
+__device__ __forceinline__ uint32_t flip_mask(uint32_t x, const ExactParams& P) {
+  const uint32_t full = P.n >= 32 ? 0xffffffffu : ((1u << P.n) - 1u);
+  uint32_t c0 = 0, c1 = 0, c2 = 0;
+  for (int o = 1; o <= P.dist; ++o) {
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+      const uint32_t v = side == 0 ? (x << o) & full : x >> o;
+      const uint32_t k0 = c0 & v;
+      c0 ^= v;
+      const uint32_t k1 = c1 & k0;
+      c1 ^= k0;
+      c2 |= k1;  // at most 6 alive neighbours: no carry out of c2
+    }
+  }
+  uint32_t m = 0;
+  for (int v = P.rule_lo; v < P.rule_hi && v < 8; ++v)
+    m |= ((v & 1) ? c0 : ~c0) & ((v & 2) ? c1 : ~c1) & ((v & 4) ? c2 : ~c2);
+  return m & full;
+}
+
+// flip condition of bit b for the amplitude x (fm = flip_mask(x) when dist <= 3)
+__device__ __forceinline__ bool may_flip(uint32_t x, uint32_t fm, int b, const ExactParams& P) {
+  if (P.dist <= 3) return (fm >> b) & 1u;
+  const int c = __popc(x & P.nmask[b]);
+  return c >= P.rule_lo && c < P.rule_hi;
+}
 
 // Scalar slots in the device scalar array.
 enum : int {
@@ -108,11 +143,11 @@ __global__ void __launch_bounds__(kExactThreads) ex_phase0(ExactParams P, PhaseG
   __syncthreads();
   for (int l = threadIdx.x; l < tsize; l += blockDim.x) {
     const long long x = tile_index(G, P.n, t, l);
+    const uint32_t fm = P.dist <= 3 ? flip_mask((uint32_t)x, P) : 0u;
     cplx<T> acc = mk<T>(0, 0);
 #pragma unroll 4
     for (int b = G.lo; b < G.lo + G.g; ++b) {
-      const int c = __popc((uint32_t)x & P.nmask[b]);
-      if (c >= P.rule_lo && c < P.rule_hi) {
+      if (may_flip((uint32_t)x, fm, b, P)) {
         const cplx<T> v = tile[l ^ (1 << (G.kl + b - G.lo))];
         acc.re += v.re;
         acc.im += v.im;
@@ -162,11 +197,11 @@ __global__ void __launch_bounds__(kExactThreads) ex_phaseH(ExactParams P, PhaseG
   T alpha_t = 0;
   for (int l = threadIdx.x; l < tsize; l += blockDim.x) {
     const long long x = tile_index(G, P.n, t, l);
+    const uint32_t fm = P.dist <= 3 ? flip_mask((uint32_t)x, P) : 0u;
     cplx<T> acc = y[x];
 #pragma unroll 4
     for (int b = G.lo; b < G.lo + G.g; ++b) {
-      const int c = __popc((uint32_t)x & P.nmask[b]);
-      if (c >= P.rule_lo && c < P.rule_hi) {
+      if (may_flip((uint32_t)x, fm, b, P)) {
         const cplx<T> v = tile[l ^ (1 << (G.kl + b - G.lo))];
         acc.re += v.re;
         acc.im += v.im;
@@ -587,6 +622,7 @@ int qca_exact_create(int n_cells, int distance, int interval_lo, int interval_hi
   E.P.rule_lo = interval_lo;
   E.P.rule_hi = interval_hi;
   E.P.dim = E.dim;
+  E.P.dist = distance;
   for (int b = 0; b < kMaxCells; ++b) E.P.nmask[b] = 0;
   for (int b = 0; b < n_cells; ++b) {
     const int i = n_cells - 1 - b;
@@ -785,6 +821,7 @@ extern "C" int qca_exact_step_noalloc(int n_cells, int distance, int interval_lo
   E.P.rule_lo = interval_lo;
   E.P.rule_hi = interval_hi;
   E.P.dim = E.dim;
+  E.P.dist = distance;
   for (int b = 0; b < kMaxCells; ++b) E.P.nmask[b] = 0;
   for (int b = 0; b < n_cells; ++b) {
     const int i = n_cells - 1 - b;

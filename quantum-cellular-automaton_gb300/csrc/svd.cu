@@ -721,19 +721,13 @@ int svd_cluster_plan(int mx, int nx, int* cs, int* cpc, size_t* smem, int* v_sme
 
 // cluster size one problem needs (0 if it does not fit); used to group problems
 template <typename T>
-int svd_cluster_size(int Dl, int Dr) {
-  const int m = 2 * Dl, n = 2 * Dr, mx = m > n ? m : n, nx = m > n ? n : m;
+int svd_cluster_size(int Dl, int Dr, int right_sweep) {
+  const int p = right_sweep ? 2 * Dl : 2 * Dr, mx = right_sweep ? 2 * Dr : 2 * Dl, nx = p < mx ? p : mx;
   int cs, cpc, vs;
   size_t sm;
   if (svd_block_plan<T>(mx, nx, &cs, &cpc, &sm, &vs)) return cs;
   if (svd_cluster_plan<T>(mx, nx, &cs, &cpc, &sm, &vs) != QCA_OK) return 0;
   return cs;
-}
-
-// shared-memory footprint check used by the host before choosing this path
-template <typename T>
-bool svd_fits(int Dl, int Dr) {
-  return svd_cluster_size<T>(Dl, Dr) > 0;
 }
 
 template <typename T>
@@ -769,9 +763,10 @@ int launch_svd(const SvdDesc<T>* d, const SvdDesc<T>* h, int nd, cudaStream_t st
   if (nd <= 0) return QCA_OK;
   int mxmax = 1, nxmax = 1;
   for (int i = 0; i < nd; ++i) {
-    const int m = 2 * h[i].Dl, n = 2 * h[i].Dr;
-    mxmax = std::max(mxmax, std::max(m, n));
-    nxmax = std::max(nxmax, std::min(m, n));
+    // Jacobi runs on X = R^H: q rows (2 Dr right, 2 Dl left), K = min(p, q) columns
+    const int p = h[i].right_sweep ? 2 * h[i].Dl : 2 * h[i].Dr, q = h[i].right_sweep ? 2 * h[i].Dr : 2 * h[i].Dl;
+    mxmax = std::max(mxmax, q);
+    nxmax = std::max(nxmax, std::min(p, q));
   }
   const int rows = (mxmax + 31) / 32;
   if (rows > 16) {
@@ -825,10 +820,8 @@ int launch_svd(const SvdDesc<T>* d, const SvdDesc<T>* h, int nd, cudaStream_t st
 
 template int launch_svd<double>(const SvdDesc<double>*, const SvdDesc<double>*, int, cudaStream_t);
 template int launch_svd<float>(const SvdDesc<float>*, const SvdDesc<float>*, int, cudaStream_t);
-template bool svd_fits<double>(int, int);
-template bool svd_fits<float>(int, int);
-template int svd_cluster_size<double>(int, int);
-template int svd_cluster_size<float>(int, int);
+template int svd_cluster_size<double>(int, int, int);
+template int svd_cluster_size<float>(int, int, int);
 
 }  // namespace qca
 

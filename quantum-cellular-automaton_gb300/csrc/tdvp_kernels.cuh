@@ -169,7 +169,7 @@ template <typename T>
 int launch_svd(const SvdDesc<T>* d, const SvdDesc<T>* h, int nd, cudaStream_t st);
 // thread-block cluster size the SVD of one (2 Dl) x (2 Dr) problem needs (0: too large)
 template <typename T>
-int svd_cluster_size(int Dl, int Dr);
+int svd_cluster_size(int Dl, int Dr, int right_sweep);
 
 // ----------------------------------------------------------------------------------
 // Householder QR with LAPACK's reflector convention (zgeqrf + zungqr):
