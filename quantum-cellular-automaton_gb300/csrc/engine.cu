@@ -512,7 +512,7 @@ struct Engine final : EngineBase {
   int check_svd(const std::vector<SvdDesc<T>>& v) const {
     const std::vector<Span> sp = spans();
     for (auto& d : v) {
-      const long long p = d.right_sweep ? 2LL * d.Dl : 2LL * d.Dr, q = d.right_sweep ? 2LL * d.Dr : 2LL * d.Dl;
+      const long long p = d.right_sweep ? 2LL * d.Dr : 2LL * d.Dl, q = d.right_sweep ? 2LL * d.Dl : 2LL * d.Dr;
       const long long K = std::min(p, q);
       if (!in_spans<T>(sp, d.theta, 4LL * d.Dl * d.Dr - 1)) return bad("svd theta");
       if (!in_spans<T>(sp, d.work, K * K - 1)) return bad("svd work");

@@ -3,18 +3,19 @@
 //   k = min{ i : ||s[i:]||_2 < eps }  capped at min(chi, len s)
 // and s renormalised (lautils.normalize, lautils.py:4-5).
 //
-// QR-preconditioned one-sided (Hestenes) Jacobi.  The matrix W = Theta on a right
-// sweep (the left factor must come out an isometry) or W = Theta^H on a left
+// QR-preconditioned one-sided (Hestenes) Jacobi.  The matrix W = Theta^H on a
+// right sweep (the left factor must come out an isometry) or W = Theta on a left
 // sweep (the right factor must) is first factored W = Q R by Householder
 // reflections (qr.cu, launched before these kernels), and the Jacobi rotations
 // run on X = R^H (q x K) with the rotations accumulated into V (K x K).  The
 // two-site matrices of TDVP have exponentially graded spectra; on them Jacobi
-// applied to W directly converges linearly and needs dozens of sweeps, while on
-// R^H, whose columns are already nearly orthogonal and graded, a handful suffice.
-// At convergence W = (Q V) Sigma (X / Sigma)^H with X = R^H V, so the site tensors
-// are written from
-//   the isometric factor Q V (column j: Q times V column j, FP32 or FP64 sums),
-//   the other factor X itself (it carries the singular values),
+// applied to the matrix directly converges linearly and needs dozens of sweeps,
+// while on R^H, whose columns are already nearly orthogonal and graded, far fewer
+// suffice.  At convergence W^H = (X / Sigma) Sigma (Q V)^H with X = R^H V, so the
+// site tensors are written from
+//   the isometric factor X / Sigma (its orthogonality is what the rotation
+//   tolerance enforces, so it holds in FP32 too),
+//   the other factor (Q V) Sigma (column j: Q times V column j),
 // with the renormalised singular values in the non-isometric factor (tdvp.py:
 // 121-122 and 141-142).  The singular values are the FP64 norms of X's columns.
 //
@@ -237,12 +238,12 @@ __device__ __forceinline__ void load_x_column(const SvdDesc<T>& D, int mx, int n
   }
 }
 
-// Shape of the preconditioned problem: W (p x q) is Theta on a right sweep and
-// Theta^H on a left sweep; Jacobi runs on X = R^H, mx = q rows and nx = K columns.
+// Shape of the preconditioned problem: W (p x q) is Theta^H on a right sweep and
+// Theta on a left sweep; Jacobi runs on X = R^H, mx = q rows and nx = K columns.
 template <typename T>
 __device__ __forceinline__ void split_shape(const SvdDesc<T>& D, int& p, int& mx, int& nx) {
-  p = D.right_sweep ? 2 * D.Dl : 2 * D.Dr;
-  mx = D.right_sweep ? 2 * D.Dr : 2 * D.Dl;
+  p = D.right_sweep ? 2 * D.Dr : 2 * D.Dl;
+  mx = D.right_sweep ? 2 * D.Dl : 2 * D.Dr;
   nx = p < mx ? p : mx;
 }
 
@@ -327,37 +328,41 @@ __device__ void svd_finish(const SvdDesc<T>& D, cg::cluster_group& cluster, int 
   const double keep = *cluster.map_shared_rank(s_keep, 0);
   const int* perm0 = cluster.map_shared_rank(perm, 0);
   const double* sn0 = cluster.map_shared_rank(snorm, 0);
-  // Kept column i (global column j = perm[i]): the isometric factor Q v_j (p rows,
-  // Q column major p x K) and the other factor x_j / ||s_kept|| (mx = q rows).
-  //   right sweep (W = Theta):   A_l[(s1,a)][i] = (Q v_j)[(s1,a)],
-  //                              A_r[s2][i][c] = conj(x_j[(s2,c)]) / keep
-  //   left sweep  (W = Theta^H): A_l[(s1,a)][i] = x_j[(s1,a)] / keep,
-  //                              A_r[s2][i][c] = conj((Q v_j)[(s2,c)])
-  const double inv_keep = keep > 0 ? 1.0 / keep : 0.0;
+  // Kept column i (global column j = perm[i], singular value sigma_j): the
+  // isometric factor x_j / sigma_j (mx = q rows) and the other factor
+  // (Q v_j) sigma_j / ||s_kept|| (p rows, Q column major p x K).
+  //   right sweep (W = Theta^H): A_l[(s1,a)][i] = x_j[(s1,a)] / sigma_j,
+  //                              A_r[s2][i][c] = conj((Q v_j)[(s2,c)]) sigma_j / keep
+  //   left sweep  (W = Theta):   A_l[(s1,a)][i] = (Q v_j)[(s1,a)] sigma_j / keep,
+  //                              A_r[s2][i][c] = conj(x_j[(s2,c)]) / sigma_j
   for (int i = 0; i < k; ++i) {
     const int j = perm0[i];
     if (!L.own(j)) continue;
     const cplx<T>* x = L.x(j);
     const cplx<T>* v = L.v(j);
+    const double sig = sn0[j];
+    const double inv = sig > 0 ? 1.0 / sig : 0.0;
+    const double sn = keep > 0 ? sig / keep : 0.0;  // renormalised singular value
     for (int row = threadIdx.x; row < p; row += blockDim.x) {
       cplx<T> u = mk<T>(0, 0);
       const cplx<T>* qr = D.qmat + row;
       for (int t = 0; t < nx; ++t) cfma(u, qr[(long long)t * p], v[t]);
-      if (D.right_sweep) {
-        D.Al[(long long)row * k + i] = u;
-      } else {
-        const int s2 = row / Dr, cc = row - s2 * Dr;
-        D.Ar[((long long)s2 * k + i) * Dr + cc] = conj(u);
-      }
-    }
-    for (int row = threadIdx.x; row < mx; row += blockDim.x) {
-      const cplx<T> u = x[row];
-      const cplx<T> w = mk<T>((T)(u.re * inv_keep), (T)(u.im * inv_keep));
+      const cplx<T> w = mk<T>((T)(u.re * sn), (T)(u.im * sn));
       if (D.right_sweep) {
         const int s2 = row / Dr, cc = row - s2 * Dr;
         D.Ar[((long long)s2 * k + i) * Dr + cc] = conj(w);
       } else {
         D.Al[(long long)row * k + i] = w;
+      }
+    }
+    for (int row = threadIdx.x; row < mx; row += blockDim.x) {
+      const cplx<T> u = x[row];
+      const cplx<T> w = mk<T>((T)(u.re * inv), (T)(u.im * inv));
+      if (D.right_sweep) {
+        D.Al[(long long)row * k + i] = w;
+      } else {
+        const int s2 = row / Dr, cc = row - s2 * Dr;
+        D.Ar[((long long)s2 * k + i) * Dr + cc] = conj(w);
       }
     }
   }
@@ -722,7 +727,7 @@ int svd_cluster_plan(int mx, int nx, int* cs, int* cpc, size_t* smem, int* v_sme
 // cluster size one problem needs (0 if it does not fit); used to group problems
 template <typename T>
 int svd_cluster_size(int Dl, int Dr, int right_sweep) {
-  const int p = right_sweep ? 2 * Dl : 2 * Dr, mx = right_sweep ? 2 * Dr : 2 * Dl, nx = p < mx ? p : mx;
+  const int p = right_sweep ? 2 * Dr : 2 * Dl, mx = right_sweep ? 2 * Dl : 2 * Dr, nx = p < mx ? p : mx;
   int cs, cpc, vs;
   size_t sm;
   if (svd_block_plan<T>(mx, nx, &cs, &cpc, &sm, &vs)) return cs;
@@ -764,7 +769,7 @@ int launch_svd(const SvdDesc<T>* d, const SvdDesc<T>* h, int nd, cudaStream_t st
   int mxmax = 1, nxmax = 1;
   for (int i = 0; i < nd; ++i) {
     // Jacobi runs on X = R^H: q rows (2 Dr right, 2 Dl left), K = min(p, q) columns
-    const int p = h[i].right_sweep ? 2 * h[i].Dl : 2 * h[i].Dr, q = h[i].right_sweep ? 2 * h[i].Dr : 2 * h[i].Dl;
+    const int p = h[i].right_sweep ? 2 * h[i].Dr : 2 * h[i].Dl, q = h[i].right_sweep ? 2 * h[i].Dl : 2 * h[i].Dr;
     mxmax = std::max(mxmax, q);
     nxmax = std::max(nxmax, std::min(p, q));
   }
@@ -834,7 +839,7 @@ template <typename T>
 static int test_svd(int Dl, int Dr, const void* theta, int chi, double eps, int max_sweeps, void* Al, void* Ar,
                     double* sv, int* k_out, cudaStream_t st) {
   using namespace qca;
-  const int p = 2 * Dl, q = 2 * Dr, K = std::min(p, q);
+  const int p = 2 * Dr, q = 2 * Dl, K = std::min(p, q);  // right sweep: W = Theta^H
   const size_t es = sizeof(cplx<T>);
   // scratch: QR work (p q + p K), tau (K), Q (p K), R (K q), V (K^2), flags, descriptors
   const size_t n_work = (size_t)p * q + (size_t)p * K, n_tau = K, n_q = (size_t)p * K, n_r = (size_t)K * q,

@@ -137,14 +137,15 @@ int launch_lz_combine(const LanczosDesc<T>* d, const LanczosDesc<T>* h, int nd, 
 // SVD of the two-site matrix by one-sided Jacobi + truncation (tdvp.py:286-296)
 // ----------------------------------------------------------------------------------
 // The split is preconditioned by a Householder QR (launch_qr, run first): the
-// matrix W = Theta (right sweep) or Theta^H (left sweep), p x q with
+// matrix W = Theta^H (right sweep) or Theta (left sweep), p x q with
 // Theta[(s1,a),(s2,c)] = theta[s1*2+s2][a][c], is factored W = Q R (Q p x K, K =
 // min(p, q)), and one-sided Jacobi runs on X = R^H (q x K), whose columns are
 // graded and nearly orthogonal, so the sweeps converge in a few rounds instead of
-// the dozens the raw, strongly graded two-site matrix needs.  With X V
-// orthogonal: W = (Q V) Sigma (X V / Sigma)^H, so the isometric factor of the
-// split is Q V (orthonormal to rounding, whatever the singular value) and the
-// other factor is X V itself, which carries Sigma.
+// the dozens the raw, strongly graded two-site matrix needs.  With X (rotated)
+// orthogonal: W^H = (X / Sigma) Sigma (Q V)^H, so the factor the sweep needs
+// isometric (A_l on a right sweep, A_r on a left one) is X / Sigma, whose
+// orthogonality the Jacobi tolerance enforces directly, and the other factor is
+// (Q V) Sigma, which carries the rounding of the accumulated rotations V.
 template <typename T>
 struct SvdDesc {
   const cplx<T>* theta;  // theta[s][a][c], s = s1*2+s2, dims (4, Dl, Dr)
@@ -155,8 +156,8 @@ struct SvdDesc {
   int right_sweep;       // 1: A_l = U, A_r = s Vh ; 0: A_l = U s, A_r = Vh
   cplx<T>* Al;           // out (2, Dl, k)
   cplx<T>* Ar;           // out (2, k, Dr)
-  const cplx<T>* qmat;   // Q of W = Q R, column major p x K (p = 2 Dl right, 2 Dr left)
-  const cplx<T>* rmat;   // R, row major K x q (q = 2 Dr right, 2 Dl left)
+  const cplx<T>* qmat;   // Q of W = Q R, column major p x K (p = 2 Dr right, 2 Dl left)
+  const cplx<T>* rmat;   // R, row major K x q (q = 2 Dl right, 2 Dr left)
   cplx<T>* work;         // V columns when they do not fit in the cluster's shared memory (K^2)
   double* sv;            // singular values (n_x), FP64
   int* k_out;            // new bond dimension
@@ -207,8 +208,8 @@ template <typename T>
 // gauge != 0: a gauge move of the mixed path (FP32 sums); 0: FP64 sums
 int launch_qr(const QrDesc<T>* d, int nd, int gauge, cudaStream_t st);
 
-// The QR that preconditions a two-site split (see SvdDesc): W = Theta (right
-// sweep, p = 2 Dl, q = 2 Dr) or Theta^H (left sweep, p = 2 Dr, q = 2 Dl) read
+// The QR that preconditions a two-site split (see SvdDesc): W = Theta^H (right
+// sweep, p = 2 Dr, q = 2 Dl) or Theta (left sweep, p = 2 Dl, q = 2 Dr) read
 // straight from theta[s1*2+s2][a][c]; Q into q_out (column major p x K), R into
 // r_out (row major K x q).  work needs p q + p K elements, tau K.
 template <typename T>
@@ -217,16 +218,16 @@ QrDesc<T> split_qr_desc(const cplx<T>* theta, int Dl, int Dr, int right_sweep, c
   QrDesc<T> d;
   memset(&d, 0, sizeof(d));
   const long long blk = (long long)Dl * Dr;
-  const int p = right_sweep ? 2 * Dl : 2 * Dr, q = right_sweep ? 2 * Dr : 2 * Dl, K = p < q ? p : q;
+  const int p = right_sweep ? 2 * Dr : 2 * Dl, q = right_sweep ? 2 * Dl : 2 * Dr, K = p < q ? p : q;
   d.in = theta;
-  if (right_sweep) {  // rows (s1, a), columns (s2, c)
+  if (!right_sweep) {  // W = Theta: rows (s1, a), columns (s2, c)
     d.rsplit = Dl;
     d.sIr1 = 2 * blk;
     d.sIr0 = Dr;
     d.csplit = Dr;
     d.sIc1 = blk;
     d.sIc = 1;
-  } else {  // rows (s2, c), columns (s1, a), conjugated
+  } else {  // W = Theta^H: rows (s2, c), columns (s1, a), conjugated
     d.rsplit = Dr;
     d.sIr1 = blk;
     d.sIr0 = 1;

@@ -93,8 +93,9 @@ def test_svd_graded_spectrum_converges(prec_name, D, decay):
     spanning 1e-12 of the largest); one-sided Jacobi on them directly needs dozens
     of sweeps.  After the QR preconditioning the split converges within the sweep
     limit, A_l is an isometry to rounding and the kept singular values are
-    accurate to rounding relative to the largest (FP64 1e-12; mixed: isometry and
-    reconstruction 2e-6, singular values 1e-6 of the largest)."""
+    accurate to rounding relative to the largest (FP64 1e-12; mixed: isometry 5e-6,
+    set by the FP32 rotation tolerance of 16 eps32, reconstruction 2e-5, singular
+    values 1e-5 of the largest)."""
     from qca_gb300 import _lib
     prec = _lib.QCA_PREC_FP64 if prec_name == "fp64" else _lib.QCA_PREC_MIXED
     rng = np.random.default_rng(D)
@@ -108,12 +109,13 @@ def test_svd_graded_spectrum_converges(prec_name, D, decay):
     if prec_name == "mixed":
         theta = theta.astype(np.complex64).astype(np.complex128)
         M = theta_matrix(theta, D, D)
-    tol = 1e-12 if prec_name == "fp64" else 2e-6
-    tol_s = 1e-12 if prec_name == "fp64" else 1e-6
+    tol_iso = 1e-12 if prec_name == "fp64" else 5e-6
+    tol_rec = 1e-12 if prec_name == "fp64" else 2e-5
+    tol_s = 1e-12 if prec_name == "fp64" else 1e-5
     Al, Ar, sv, k = run_svd(prec, D, D, theta)  # raises on QCA_ERR_NOT_CONVERGED
     ref = np.linalg.svd(M, compute_uv=False)
     assert np.abs(sv[:k] - ref[:k]).max() <= tol_s * ref[0]
     Ul = Al.reshape(n, k)
-    assert np.abs(Ul.conj().T @ Ul - np.eye(k)).max() <= tol
+    assert np.abs(Ul.conj().T @ Ul - np.eye(k)).max() <= tol_iso
     R = np.einsum("sai,tic->satc", Al, Ar).reshape(n, n)
-    assert np.linalg.norm(R - M / np.linalg.norm(M)) <= 10 * tol + np.sqrt(np.sum(ref[k:] ** 2))
+    assert np.linalg.norm(R - M / np.linalg.norm(M)) <= tol_rec + np.sqrt(np.sum(ref[k:] ** 2))
