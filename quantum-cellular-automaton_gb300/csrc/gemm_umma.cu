@@ -15,11 +15,7 @@
 //
 // A CTA (256 threads) computes 128 x 64 complex tiles (128 x 128 real accumulators);
 // the kernel is persistent, one CTA per SM walking the tiles b, b + grid, ..., and
-// its stage pipeline runs on across tile boundaries.  The operands of the next three K
-// stages are in flight from global memory at all times: every thread copies its
-// own elements (cp.async, 8 bytes each, out-of-range elements zero-filled) into a
-// ring of raw complex64 stages, so the gathers' latency is hidden behind three
-// stages of MMAs instead of one.  Per K stage of 16 complex elements all threads convert the
+// its stage pipeline runs on across tile boundaries.  Per K stage of 16 complex elements all threads convert the
 // stage's operands and store them in shared memory in the canonical K-major layout
 // without swizzle (core matrices of 8 rows x 16 bytes): a thread owns one row and
 // four consecutive K elements and writes whole 16-byte core-matrix rows, lanes on
@@ -39,11 +35,7 @@ constexpr int kUmBM = 128, kUmBN = 64, kUmBK = 16;   // complex tile and K stage
 constexpr int kUmThreads = 256;
 constexpr uint32_t kUmPlane = 128u * 2 * kUmBK * 4;  // one operand plane: 128 rows x 32 tf32
 constexpr uint32_t kUmStage = 4 * kUmPlane;          // A hi, A lo, B hi, B lo
-// raw complex64 operands of one K stage as loaded from global memory (cp.async):
-// A [row 0..127][k 0..15], then B [column 0..63][k 0..15]
-constexpr uint32_t kUmRawA = kUmBM * kUmBK * 8, kUmRaw = kUmRawA + kUmBN * kUmBK * 8;
-constexpr int kUmRing = 3;                           // K stages in flight from global memory
-constexpr size_t kUmSmem = 2 * kUmStage + kUmRing * kUmRaw + 1024;  // split stages + raw ring + slack
+constexpr size_t kUmSmem = 2 * kUmStage + 1024;      // two stages + alignment slack
 constexpr int kUmWaitLimit = 1 << 20;
 
 // instruction descriptor, kind::tf32: D f32 (bits 4-5 = 1), A and B tf32 (bits 7-9,
@@ -76,18 +68,6 @@ __device__ __forceinline__ uint32_t um_tf32(float x) {
 // core matrices along K at 128 B, rows of a core matrix at 16 B
 __device__ __forceinline__ uint32_t um_off(int row, int kp) {
   return (uint32_t)((row >> 3) * 1024 + (kp >> 2) * 128 + (row & 7) * 16 + (kp & 3) * 4);
-}
-
-// 8-byte asynchronous copy global -> shared; src_size 0 zero-fills the destination
-__device__ __forceinline__ void um_cp8(uint32_t dst, const void* src, bool valid) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(dst), "l"(src), "r"(valid ? 8 : 0)
-               : "memory");
-}
-
-__device__ __forceinline__ cplx<float> um_ld8(uint32_t addr) {
-  float re, im;
-  asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(re), "=f"(im) : "r"(addr) : "memory");
-  return mk<float>(re, im);
 }
 
 __device__ __forceinline__ void um_st4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
@@ -261,53 +241,37 @@ __global__ void __launch_bounds__(kUmThreads, 1) gemm_umma_grouped(const GemmDes
 
   // staging tasks: A rows m (2 per thread) and B columns n (1 per thread), each with
   // the four consecutive K elements 4 kg .. 4 kg + 3 of the stage; lanes run over
-  // consecutive rows, so every 16-byte shared store of a warp hits distinct banks.
-  // A thread copies exactly the elements it later converts (cp.async into the raw
-  // ring, kUmRing stages ahead), so its own cp.async.wait_group is the only
-  // synchronisation the raw ring needs.
+  // consecutive rows, so every 16-byte shared store of a warp hits distinct banks
   const int am = tid & (kUmBM - 1), akg = tid >> 7;  // task q: kg = akg + 2 q
   const int bn = tid & (kUmBN - 1), bkg = tid >> 6;
-  const uint32_t rbase = sbase + 2 * kUmStage;       // raw ring
-  uint32_t conj_bits = 0;                            // bit 2 r: conj A, 2 r + 1: conj B of ring slot r
-  auto fetch = [&](const UmCur& c, int slot) {
+  cplx<float> ra[2][4], rb[4];
+  bool conj_a = false, conj_b = false;  // of the fetched stage
+  auto fetch = [&](const UmCur& c) {
     const GemmDesc<float>& D = *c.T.D;
     const int gg = c.s / c.T.ksl, k0 = (c.s - gg * c.T.ksl) * kUmBK;
     const cplx<float>* Ag = c.T.A + gg * D.sAg;
     const cplx<float>* Bg = c.T.B + gg * D.sBg;
     const int M = D.M, N = D.N, K = D.K;
     const long long sAm = D.sAm, sAk = D.sAk, sBk = D.sBk, sBn = D.sBn;
-    const uint32_t ra = rbase + slot * kUmRaw, rb = ra + kUmRawA;
     const int m = c.T.m0 + am;
 #pragma unroll
     for (int q = 0; q < 2; ++q)
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
-        const int kl = 4 * (akg + 2 * q) + i, k = k0 + kl;
-        const bool in = m < M && k < K;
-        // out-of-range elements are zero-filled (source size 0; the address is not read)
-        um_cp8(ra + (uint32_t)(am * kUmBK + kl) * 8u, in ? Ag + m * sAm + k * sAk : Ag, in);
+        const int k = k0 + 4 * (akg + 2 * q) + i;
+        ra[q][i] = (m < M && k < K) ? Ag[m * sAm + k * sAk] : mk<float>(0.f, 0.f);
       }
     const int n = c.T.n0 + bn;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      const int kl = 4 * bkg + i, k = k0 + kl;
-      const bool in = n < N && k < K;
-      um_cp8(rb + (uint32_t)(bn * kUmBK + kl) * 8u, in ? Bg + k * sBk + n * sBn : Bg, in);
+      const int k = k0 + 4 * bkg + i;
+      rb[i] = (n < N && k < K) ? Bg[k * sBk + n * sBn] : mk<float>(0.f, 0.f);
     }
-    const uint32_t bits = (D.conjA != 0 ? 1u : 0u) | (D.conjB != 0 ? 2u : 0u);
-    conj_bits = (conj_bits & ~(3u << (2 * slot))) | (bits << (2 * slot));
+    conj_a = D.conjA != 0;
+    conj_b = D.conjB != 0;
   };
-  auto stash = [&](int buf, int slot) {
+  auto stash = [&](int buf) {
     const uint32_t st0 = sbase + buf * kUmStage;
-    const uint32_t ra_s = rbase + slot * kUmRaw, rb_s = ra_s + kUmRawA;
-    const bool conj_a = (conj_bits >> (2 * slot)) & 1u, conj_b = (conj_bits >> (2 * slot + 1)) & 1u;
-    cplx<float> ra[2][4], rb[4];
-#pragma unroll
-    for (int q = 0; q < 2; ++q)
-#pragma unroll
-      for (int i = 0; i < 4; ++i) ra[q][i] = um_ld8(ra_s + (uint32_t)(am * kUmBK + 4 * (akg + 2 * q) + i) * 8u);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) rb[i] = um_ld8(rb_s + (uint32_t)(bn * kUmBK + 4 * bkg + i) * 8u);
     const uint32_t ah = st0, al = st0 + kUmPlane, bh = st0 + 2 * kUmPlane, bl = st0 + 3 * kUmPlane;
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
@@ -394,23 +358,17 @@ __global__ void __launch_bounds__(kUmThreads, 1) gemm_umma_grouped(const GemmDes
   };
 
   UmCur S = F;  // stage to stash and multiply
-  for (int r = 0; r < kUmRing; ++r) {  // prologue: the first kUmRing stages in flight
-    if (F.s >= 0) fetch(F, r);
-    asm volatile("cp.async.commit_group;" ::: "memory");
-    um_advance(s_tb, descs, nd, total, F);
-  }
+  fetch(F);
+  um_advance(s_tb, descs, nd, total, F);
   UmCur R;  // stage to read out (previous iteration's)
   R.s = -1;
   int g = 0;
   for (; S.s >= 0; ++g) {
-    const int buf = g & 1, slot = g % kUmRing;
+    const int buf = g & 1;
     // buffer buf was last read by the MMAs of stage g - 2, whose completion every
-    // thread observed in the read-out of stage g - 2; this thread's copies of stage
-    // g are the oldest kUmRing groups' first
-    asm volatile("cp.async.wait_group %0;" ::"n"(kUmRing - 1) : "memory");
-    stash(buf, slot);
-    if (F.s >= 0) fetch(F, slot);  // refill the slot just converted: kUmRing stages ahead
-    asm volatile("cp.async.commit_group;" ::: "memory");
+    // thread observed in the read-out of stage g - 2
+    stash(buf);
+    if (F.s >= 0) fetch(F);  // global loads in flight during the MMAs
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -435,10 +393,9 @@ __global__ void __launch_bounds__(kUmThreads, 1) gemm_umma_grouped(const GemmDes
       if (R.s == R.T.nst - 1) epilogue(R.T);
     }
     R = S;
-    um_advance(s_tb, descs, nd, total, S);
+    S = F;
     um_advance(s_tb, descs, nd, total, F);
   }
-  asm volatile("cp.async.wait_all;" ::: "memory");
   // the last stage issued (R, global index g - 1) ends the CTA's last tile
   if (ok) readout(g - 1);
   epilogue(R.T);
