@@ -515,8 +515,6 @@ struct Engine final : EngineBase {
       const long long p = d.right_sweep ? 2LL * d.Dr : 2LL * d.Dl, q = d.right_sweep ? 2LL * d.Dl : 2LL * d.Dr;
       const long long K = std::min(p, q);
       if (!in_spans<T>(sp, d.theta, 4LL * d.Dl * d.Dr - 1)) return bad("svd theta");
-      if (!in_spans<T>(sp, d.work, K * K - 1)) return bad("svd work");
-      if (!in_spans<T>(sp, d.qmat, p * K - 1)) return bad("svd Q");
       if (!in_spans<T>(sp, d.rmat, K * q - 1)) return bad("svd R");
       if (!in_spans<T>(sp, d.Al, 2LL * d.Dl * d.kmax - 1)) return bad("svd Al");
       if (!in_spans<T>(sp, d.Ar, 2LL * d.kmax * d.Dr - 1)) return bad("svd Ar");
@@ -1117,14 +1115,9 @@ struct Engine final : EngineBase {
         d.right_sweep = c->dir == 0;
         d.Al = c->alt(l);
         d.Ar = c->alt(r);
-        // workspace: Q (p K <= 4 cmax^2), R (K q), V (K^2); the QR's own work in qrw
-        const long long c2 = 4LL * c->cmax * c->cmax;
-        cplx<T>* qbuf = c->svdw;
-        cplx<T>* rbuf = c->svdw + c2;
-        d.qmat = qbuf;
-        d.rmat = rbuf;
-        d.work = c->svdw + 2 * c2;
-        spre.push_back(split_qr_desc<T>(c->theta, d.Dl, d.Dr, d.right_sweep, c->qrw, c->qrtau, qbuf, rbuf));
+        // R of the preconditioning QR (K q <= 4 cmax^2) in svdw; the QR's own work in qrw
+        d.rmat = c->svdw;
+        spre.push_back(split_qr_desc<T>(c->theta, d.Dl, d.Dr, d.right_sweep, c->qrw, c->qrtau, c->svdw));
         d.sv = c->sv;
         d.k_out = c->iflags;
         d.discarded = c->dscal;
@@ -1875,7 +1868,7 @@ static void plan_chain(const qca_chain_desc* d, int mmax, Layout& Lo, std::vecto
   put(es * nmax * (mmax + 1));              // basis
   put(es * tmax);                           // t1
   put(es * tmax);                           // t2
-  put(es * 12ull * cmax * cmax);            // svd work: Q (p K), R (K q), V (K^2); p, q, K <= 2 cmax
+  put(es * 4ull * cmax * cmax);             // svd work: R (K q), q, K <= 2 cmax
   put(es * (8ull * cmax * cmax + 2 * cmax));  // qr work (m*n + m*m), m <= 2 cmax, n <= 2 cmax
   put(es * 2 * cmax);                       // qr tau
   put(es * (size_t)cmax * cmax * 2);        // cbuf

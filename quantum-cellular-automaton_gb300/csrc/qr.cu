@@ -109,13 +109,13 @@ __global__ void __launch_bounds__(kQrThreads) qr_kernel(const QrDesc<T>* __restr
     }
     __syncthreads();
   }
-  // Q = H_0 ... H_{K-1} [I]_{:, :qc}
-  for (long long e = threadIdx.x; e < (long long)m * qc; e += blockDim.x) {
+  // Q = H_0 ... H_{K-1} [I]_{:, :qc}, only when it is asked for
+  for (long long e = threadIdx.x; D.q && e < (long long)m * qc; e += blockDim.x) {
     const int c = (int)(e / m), r = (int)(e - (long long)c * m);
     Q[e] = mk<T>(r == c ? (T)1 : (T)0, (T)0);
   }
   __syncthreads();
-  for (int k = K - 1; k >= 0; --k) {
+  for (int k = D.q ? K - 1 : -1; k >= 0; --k) {
     const cplx<T> t = D.tau[k];
     const double tr = t.re, ti = t.im;
     if (tr == 0.0 && ti == 0.0) continue;

@@ -7,15 +7,17 @@
 // right sweep (the left factor must come out an isometry) or W = Theta on a left
 // sweep (the right factor must) is first factored W = Q R by Householder
 // reflections (qr.cu, launched before these kernels), and the Jacobi rotations
-// run on X = R^H (q x K) with the rotations accumulated into V (K x K).  The
-// two-site matrices of TDVP have exponentially graded spectra; on them Jacobi
-// applied to the matrix directly converges linearly and needs dozens of sweeps,
-// while on R^H, whose columns are already nearly orthogonal and graded, far fewer
-// suffice.  At convergence W^H = (X / Sigma) Sigma (Q V)^H with X = R^H V, so the
+// run on X = R^H (q x K).  The two-site matrices of TDVP have exponentially
+// graded spectra; on them Jacobi applied to the matrix directly converges
+// linearly and needs dozens of sweeps, while on R^H, whose columns are already
+// nearly orthogonal and graded, far fewer suffice.  At convergence (X = R^H V, V
+// the product of the rotations) W^H = U Sigma (Q V)^H with U = X / Sigma, so the
 // site tensors are written from
-//   the isometric factor X / Sigma (its orthogonality is what the rotation
+//   the isometric factor U = X / Sigma (its orthogonality is what the rotation
 //   tolerance enforces, so it holds in FP32 too),
-//   the other factor (Q V) Sigma (column j: Q times V column j),
+//   the other factor W U = (Q V) Sigma, one product with the two-site matrix per
+//   kept column, so that neither Q nor V is ever formed and the rotations only
+//   touch X,
 // with the renormalised singular values in the non-isometric factor (tdvp.py:
 // 121-122 and 141-142).  The singular values are the FP64 norms of X's columns.
 //
@@ -186,8 +188,7 @@ __device__ __forceinline__ void pair_gram(const cplx<T> (&ru)[RPL], const cplx<T
   gi = __shfl_sync(0xffffffffu, i, 0);
 }
 
-// One Jacobi rotation of the column pair (xu, xv) of X, applied to (vu, vv) of V,
-// all held in registers.  The squared column norms and the inner product are
+// One Jacobi rotation of the column pair (xu, xv) of X, held in registers.  The squared column norms and the inner product are
 // evaluated afresh from the registers for every pair: norms carried from earlier
 // rotations in closed form drift (by the rounding of every update, and badly after
 // cancellation), and a rotation angle computed from drifted norms leaves an inner
@@ -197,8 +198,8 @@ __device__ __forceinline__ void pair_gram(const cplx<T> (&ru)[RPL], const cplx<T
 // tolerance or one column is at the rounding floor of the matrix.
 //   x_p' = c x_p - s e^{-i phi} x_q ;  x_q' = s e^{i phi} x_p + c x_q   (unitary)
 template <typename T, int RPL>
-__device__ __forceinline__ bool jacobi_rotate(cplx<T> (&xu)[RPL], cplx<T> (&xv)[RPL], cplx<T> (&vu)[RPL],
-                                              cplx<T> (&vv)[RPL], T& al, T& be, double tol, T floor2) {
+__device__ __forceinline__ bool jacobi_rotate(cplx<T> (&xu)[RPL], cplx<T> (&xv)[RPL], T& al, T& be, double tol,
+                                              T floor2) {
   T gr, gi;
   pair_gram<T, RPL>(xu, xv, al, be, gr, gi);
   const T g = sqrt(gr * gr + gi * gi);
@@ -215,9 +216,6 @@ __device__ __forceinline__ bool jacobi_rotate(cplx<T> (&xu)[RPL], cplx<T> (&xv)[
     const cplx<T> a = xu[r], b = xv[r];
     xu[r] = c * a + smq * b;
     xv[r] = spq * a + c * b;
-    const cplx<T> va = vu[r], vb = vv[r];
-    vu[r] = c * va + smq * vb;
-    vv[r] = spq * va + c * vb;
   }
   al = fmax(al - t * g, (T)0);
   be = fmax(be + t * g, (T)0);
@@ -329,30 +327,43 @@ __device__ void svd_finish(const SvdDesc<T>& D, cg::cluster_group& cluster, int 
   const int* perm0 = cluster.map_shared_rank(perm, 0);
   const double* sn0 = cluster.map_shared_rank(snorm, 0);
   // Kept column i (global column j = perm[i], singular value sigma_j): the
-  // isometric factor x_j / sigma_j (mx = q rows) and the other factor
-  // (Q v_j) sigma_j / ||s_kept|| (p rows, Q column major p x K).
-  //   right sweep (W = Theta^H): A_l[(s1,a)][i] = x_j[(s1,a)] / sigma_j,
-  //                              A_r[s2][i][c] = conj((Q v_j)[(s2,c)]) sigma_j / keep
-  //   left sweep  (W = Theta):   A_l[(s1,a)][i] = (Q v_j)[(s1,a)] sigma_j / keep,
-  //                              A_r[s2][i][c] = conj(x_j[(s2,c)]) / sigma_j
+  // isometric factor u_j = x_j / sigma_j (mx = q rows) and the other factor
+  // W u_j / ||s_kept|| (p rows): with X orthogonal, W^H = U Sigma (Q V)^H gives
+  // W u_j = (Q V)_j sigma_j, so neither Q nor the accumulated rotations are needed.
+  //   right sweep (W = Theta^H): A_l[(s1,a)][i] = u_j[(s1,a)],
+  //                              A_r[s2][i][c] = conj((W u_j)[(s2,c)]) / keep
+  //   left sweep  (W = Theta):   A_l[(s1,a)][i] = (W u_j)[(s1,a)] / keep,
+  //                              A_r[s2][i][c] = conj(u_j[(s2,c)])
+  const int Dl = D.Dl;
+  const long long blk = (long long)Dl * Dr;
   for (int i = 0; i < k; ++i) {
     const int j = perm0[i];
     if (!L.own(j)) continue;
     const cplx<T>* x = L.x(j);
-    const cplx<T>* v = L.v(j);
     const double sig = sn0[j];
     const double inv = sig > 0 ? 1.0 / sig : 0.0;
-    const double sn = keep > 0 ? sig / keep : 0.0;  // renormalised singular value
+    const double f = keep > 0 ? inv / keep : 0.0;
     for (int row = threadIdx.x; row < p; row += blockDim.x) {
-      cplx<T> u = mk<T>(0, 0);
-      const cplx<T>* qr = D.qmat + row;
-      for (int t = 0; t < nx; ++t) cfma(u, qr[(long long)t * p], v[t]);
-      const cplx<T> w = mk<T>((T)(u.re * sn), (T)(u.im * sn));
+      cplx<T> acc = mk<T>(0, 0);
       if (D.right_sweep) {
+        // (Theta^H x)[(s2,c)] = sum_{s1,a} conj(theta[s1*2+s2][a][c]) x[(s1,a)]
         const int s2 = row / Dr, cc = row - s2 * Dr;
+        for (int s1 = 0; s1 < 2; ++s1) {
+          const cplx<T>* th = D.theta + (long long)(s1 * 2 + s2) * blk + cc;
+          const cplx<T>* xs = x + s1 * Dl;
+          for (int a = 0; a < Dl; ++a) cfma_conj(acc, th[(long long)a * Dr], xs[a]);
+        }
+        const cplx<T> w = mk<T>((T)(acc.re * f), (T)(acc.im * f));
         D.Ar[((long long)s2 * k + i) * Dr + cc] = conj(w);
       } else {
-        D.Al[(long long)row * k + i] = w;
+        // (Theta x)[(s1,a)] = sum_{s2,c} theta[s1*2+s2][a][c] x[(s2,c)]
+        const int s1 = row / Dl, a = row - s1 * Dl;
+        for (int s2 = 0; s2 < 2; ++s2) {
+          const cplx<T>* th = D.theta + (long long)(s1 * 2 + s2) * blk + (long long)a * Dr;
+          const cplx<T>* xs = x + s2 * Dr;
+          for (int c = 0; c < Dr; ++c) cfma(acc, th[c], xs[c]);
+        }
+        D.Al[(long long)row * k + i] = mk<T>((T)(acc.re * f), (T)(acc.im * f));
       }
     }
     for (int row = threadIdx.x; row < mx; row += blockDim.x) {
@@ -373,11 +384,9 @@ __device__ void svd_finish(const SvdDesc<T>& D, cg::cluster_group& cluster, int 
 template <typename T>
 struct SlabLoc {
   const cplx<T>* X;
-  const cplx<T>* V;
   int cpc, mx, nx, rank;
   __device__ bool own(int j) const { return j / cpc == rank; }
   __device__ const cplx<T>* x(int j) const { return X + (long long)(j % cpc) * mx; }
-  __device__ const cplx<T>* v(int j) const { return V + (long long)(j % cpc) * nx; }
 };
 
 // blocks of svd_block_kernel at their sweep-start positions: block be sits in the
@@ -385,21 +394,16 @@ struct SlabLoc {
 template <typename T>
 struct BlockLoc {
   const cplx<T>* X;   // [slot][b][mx]
-  const cplx<T>* V;   // [slot][b][nx], or null: V column j at Vg + j nx
-  const cplx<T>* Vg;
   int P, b, mx, nx, rank;
   __device__ int blk(int j) const { return j / b; }
   __device__ int slot(int j) const { return blk(j) < P ? 0 : 1; }
   __device__ bool own(int j) const { return (blk(j) < P ? blk(j) : 2 * P - 1 - blk(j)) == rank; }
   __device__ const cplx<T>* x(int j) const { return X + ((long long)slot(j) * b + j % b) * mx; }
-  __device__ const cplx<T>* v(int j) const {
-    return V ? V + ((long long)slot(j) * b + j % b) * nx : Vg + (long long)j * nx;
-  }
 };
 
 template <typename T, int RPL>
 __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<T>* __restrict__ descs, int cs,
-                                                                  int cpc, int v_smem) {
+                                                                  int cpc) {
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
   const SvdDesc<T>& D = descs[blockIdx.x / cs];
@@ -414,13 +418,9 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
   __shared__ double red[33];
   int p, mx, nx;
   split_shape(D, p, mx, nx);
-  // V columns: after X in shared memory, or slot-major in the global workspace
-  cplx<T>* Vloc = v_smem ? Xloc + (long long)cpc * mx : D.work + (long long)rank * cpc * nx;
   for (int lc = 0; lc < cpc; ++lc) {
     const int col = rank * cpc + lc;
     if (col >= nx) break;
-    for (int row = threadIdx.x; row < nx; row += blockDim.x)
-      Vloc[(long long)lc * nx + row] = mk<T>(row == col ? (T)1 : (T)0, (T)0);
     load_x_column(D, mx, nx, col, Xloc + (long long)lc * mx);
   }
   if (threadIdx.x < 2) s_flag[threadIdx.x] = 0;
@@ -468,25 +468,17 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
         }
         cplx<T>* xp = cluster.map_shared_rank(Xloc, p / cpc) + (long long)(p % cpc) * mx;
         cplx<T>* xq = cluster.map_shared_rank(Xloc, q / cpc) + (long long)(q % cpc) * mx;
-        cplx<T>* vp = (v_smem ? cluster.map_shared_rank(Xloc, p / cpc) + (long long)cpc * mx
-                              : D.work + (long long)(p / cpc) * cpc * nx) + (long long)(p % cpc) * nx;
-        cplx<T>* vq = (v_smem ? cluster.map_shared_rank(Xloc, q / cpc) + (long long)cpc * mx
-                              : D.work + (long long)(q / cpc) * cpc * nx) + (long long)(q % cpc) * nx;
-        // both columns of X and of V staged in registers in one round of (possibly
-        // remote) loads; the rotation in the working precision T (the singular values
-        // are re-evaluated in FP64 after convergence)
-        cplx<T> ru[RPL], rv[RPL], wu[RPL], wv[RPL];
+        // both columns staged in registers in one round of (possibly remote) loads;
+        // the rotation in the working precision T (the singular values are
+        // re-evaluated in FP64 after convergence)
+        cplx<T> ru[RPL], rv[RPL];
         col_load<T, RPL>(xp, mx, ru);
         col_load<T, RPL>(xq, mx, rv);
-        col_load<T, RPL>(vp, nx, wu);
-        col_load<T, RPL>(vq, nx, wv);
         T al, be;
-        if (!jacobi_rotate<T, RPL>(ru, rv, wu, wv, al, be, tol, floor2)) continue;
+        if (!jacobi_rotate<T, RPL>(ru, rv, al, be, tol, floor2)) continue;
         rotated = 1;
         col_store<T, RPL>(xp, mx, ru);
         col_store<T, RPL>(xq, mx, rv);
-        col_store<T, RPL>(vp, nx, wu);
-        col_store<T, RPL>(vq, nx, wv);
       }
       cluster.sync();
     }
@@ -497,13 +489,12 @@ __global__ void __launch_bounds__(kSvdThreads) svd_cluster_kernel(const SvdDesc<
     if (rank == 0 && threadIdx.x == 0) s_flag[par] = 0;
     if (!any) break;
   }
-  const SlabLoc<T> L{Xloc, Vloc, cpc, mx, nx, rank};
+  const SlabLoc<T> L{Xloc, cpc, mx, nx, rank};
   svd_finish<T>(D, cluster, rank, L, p, mx, nx, sweep, floor2, snorm, perm, &s_k, &s_keep);
 }
 
 template <typename T, int RPL>
-__global__ void __launch_bounds__(kSvdThreads) svd_block_kernel(const SvdDesc<T>* __restrict__ descs, int P,
-                                                                int v_smem) {
+__global__ void __launch_bounds__(kSvdThreads) svd_block_kernel(const SvdDesc<T>* __restrict__ descs, int P) {
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
   const SvdDesc<T>& D = descs[blockIdx.x / P];
@@ -519,15 +510,9 @@ __global__ void __launch_bounds__(kSvdThreads) svd_block_kernel(const SvdDesc<T>
   split_shape(D, p, mx, nx);
   const int n2 = 2 * P;                // blocks (tournament players)
   const int b = (nx + n2 - 1) / n2;    // columns per block (<= kSvdBlk)
-  // slots [generation][top/bottom][b columns]: X (mx each), then V (nx each) when it
-  // fits, else V column j stays at D.work + j nx (never moved)
+  // slots [generation][top/bottom][b columns] of mx elements
   cplx<T>* Xs = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* Vs = v_smem ? Xs + 4LL * b * mx : nullptr;
-  cplx<T>* Vg = D.work;
   auto xs = [&](int g, int s, int j) { return Xs + ((long long)(g * 2 + s) * b + j) * mx; };
-  auto vc = [&](int g, int s, int j, int gid) {
-    return v_smem ? Vs + ((long long)(g * 2 + s) * b + j) * nx : Vg + (long long)gid * nx;
-  };
   // block at ring position pos in block round r (circle method, position 0 fixed)
   auto player = [&](int pos, int r) { return pos == 0 ? 0 : 1 + (pos - 1 + r) % (n2 - 1); };
   for (int s = 0; s < 2; ++s) {
@@ -535,11 +520,6 @@ __global__ void __launch_bounds__(kSvdThreads) svd_block_kernel(const SvdDesc<T>
     for (int j = 0; j < b; ++j) {
       const int col = be * b + j;
       load_x_column(D, mx, nx, col, xs(0, s, j));
-      if (col < nx || v_smem) {
-        cplx<T>* v = vc(0, s, j, col);
-        for (int row = threadIdx.x; row < nx; row += blockDim.x)
-          v[row] = mk<T>(row == col ? (T)1 : (T)0, (T)0);
-      }
     }
   }
   if (threadIdx.x < 2) s_flag[threadIdx.x] = 0;
@@ -586,18 +566,14 @@ __global__ void __launch_bounds__(kSvdThreads) svd_block_kernel(const SvdDesc<T>
             const int bl = s == 0 ? bt : bb;
             const int gp = bl * b + p, gq = bl * b + q;
             if (gp >= nx || gq >= nx) continue;
-            cplx<T> xu[RPL], xv[RPL], vu[RPL], vv[RPL];
+            cplx<T> xu[RPL], xv[RPL];
             col_load<T, RPL>(xs(gen, s, p), mx, xu);
             col_load<T, RPL>(xs(gen, s, q), mx, xv);
-            col_load<T, RPL>(vc(gen, s, p, gp), nx, vu);
-            col_load<T, RPL>(vc(gen, s, q, gq), nx, vv);
             T al, be;
-            if (!jacobi_rotate<T, RPL>(xu, xv, vu, vv, al, be, tol, floor2)) continue;
+            if (!jacobi_rotate<T, RPL>(xu, xv, al, be, tol, floor2)) continue;
             rotated = 1;
             col_store<T, RPL>(xs(gen, s, p), mx, xu);
             col_store<T, RPL>(xs(gen, s, q), mx, xv);
-            col_store<T, RPL>(vc(gen, s, p, gp), nx, vu);
-            col_store<T, RPL>(vc(gen, s, q, gq), nx, vv);
           }
           __syncthreads();
         }
@@ -607,36 +583,28 @@ __global__ void __launch_bounds__(kSvdThreads) svd_block_kernel(const SvdDesc<T>
         // meets bottom column (w + i) mod b in inner round i
         const int ga = bt * b + wid;
         const bool act = wid < b && ga < nx;
-        cplx<T> xu[RPL], vu[RPL];
+        cplx<T> xu[RPL];
         T al = 0;
-        if (act) {
-          col_load<T, RPL>(xs(gen, 0, wid), mx, xu);
-          col_load<T, RPL>(vc(gen, 0, wid, ga), nx, vu);
-        }
+        if (act) col_load<T, RPL>(xs(gen, 0, wid), mx, xu);
         bool dirty = false;
         for (int i = 0; i < b; ++i) {
           if (act) {
             const int j = (wid + i) % b;
             const int gb = bb * b + j;
             if (gb < nx) {
-              cplx<T> xv[RPL], vv[RPL];
+              cplx<T> xv[RPL];
               col_load<T, RPL>(xs(gen, 1, j), mx, xv);
-              col_load<T, RPL>(vc(gen, 1, j, gb), nx, vv);
               T be;
-              if (jacobi_rotate<T, RPL>(xu, xv, vu, vv, al, be, tol, floor2)) {
+              if (jacobi_rotate<T, RPL>(xu, xv, al, be, tol, floor2)) {
                 rotated = 1;
                 dirty = true;
                 col_store<T, RPL>(xs(gen, 1, j), mx, xv);
-                col_store<T, RPL>(vc(gen, 1, j, gb), nx, vv);
               }
             }
           }
           __syncthreads();
         }
-        if (dirty) {
-          col_store<T, RPL>(xs(gen, 0, wid), mx, xu);
-          col_store<T, RPL>(vc(gen, 0, wid, ga), nx, vu);
-        }
+        if (dirty) col_store<T, RPL>(xs(gen, 0, wid), mx, xu);
       }
       // move the blocks one position along the ring: position p takes the block of
       // position p + 1, position 2P - 1 the block of position 1, position 0 keeps its
@@ -653,11 +621,6 @@ __global__ void __launch_bounds__(kSvdThreads) svd_block_kernel(const SvdDesc<T>
           const cplx<T>* src = cluster.map_shared_rank(xs(gen, ss, 0), sr);
           cplx<T>* dst = xs(ng, s, 0);
           for (int e = threadIdx.x; e < b * mx; e += blockDim.x) dst[e] = src[e];
-          if (v_smem) {
-            const cplx<T>* vsrc = cluster.map_shared_rank(vc(gen, ss, 0, 0), sr);
-            cplx<T>* vdst = vc(ng, s, 0, 0);
-            for (int e = threadIdx.x; e < b * nx; e += blockDim.x) vdst[e] = vsrc[e];
-          }
         }
         __syncthreads();
         gen = ng;
@@ -671,52 +634,40 @@ __global__ void __launch_bounds__(kSvdThreads) svd_block_kernel(const SvdDesc<T>
     if (!any) break;
   }
   // after a whole sweep (2P - 1 moves) every block is back at its starting position
-  const BlockLoc<T> L{xs(gen, 0, 0), v_smem ? vc(gen, 0, 0, 0) : nullptr, Vg, P, b, mx, nx, rank};
+  const BlockLoc<T> L{xs(gen, 0, 0), P, b, mx, nx, rank};
   svd_finish<T>(D, cluster, rank, L, p, mx, nx, sweep, floor2, snorm, perm, &s_k, &s_keep);
 }
 
 // block kernel geometry: P CTAs (power of two, P * 32 >= nx where possible), blocks of
 // b <= 16 columns, X (and V when it fits) double-buffered in shared memory
 template <typename T>
-bool svd_block_plan(int mx, int nx, int* P_out, int* b_out, size_t* smem, int* v_smem) {
+bool svd_block_plan(int mx, int nx, int* P_out, int* b_out, size_t* smem) {
   if (mx > 256) return false;
   int P = 1;
   while (P * 32 < nx && P < 16) P *= 2;
   const int b = (nx + 2 * P - 1) / (2 * P);
   if (b > kSvdBlk) return false;
-  const size_t es = sizeof(cplx<T>);
-  const size_t xb = 4ull * b * mx * es, vb = 4ull * b * nx * es;
-  if (xb + vb <= kSvdSmem) {
-    *v_smem = 1;
-    *smem = xb + vb;
-  } else if (xb <= kSvdSmem) {
-    *v_smem = 0;
-    *smem = xb;
-  } else {
-    return false;
-  }
+  const size_t xb = 4ull * b * mx * sizeof(cplx<T>);  // two generations x two slots
+  if (xb > kSvdSmem) return false;
   *P_out = P;
   *b_out = b;
+  *smem = xb;
   return true;
 }
 
 template <typename T>
-int svd_cluster_plan(int mx, int nx, int* cs, int* cpc, size_t* smem, int* v_smem) {
-  const size_t es = sizeof(cplx<T>);
+int svd_cluster_plan(int mx, int nx, int* cs, int* cpc, size_t* smem) {
   const size_t limit = 200 * 1024;
   const int pairs = (nx + 1) / 2, warps = kSvdThreads / 32;
-  for (int vs = 1; vs >= 0; --vs) {
-    for (int c = 1; c <= 16; c *= 2) {
-      const int per = (nx + c - 1) / c;
-      const size_t bytes = (size_t)per * (mx + (vs ? nx : 0)) * es;
-      // enough warps in the cluster for one column pair each per round
-      if (bytes <= limit && (c * warps >= pairs || c == 16)) {
-        *cs = c;
-        *cpc = per;
-        *smem = bytes;
-        *v_smem = vs;
-        return QCA_OK;
-      }
+  for (int c = 1; c <= 16; c *= 2) {
+    const int per = (nx + c - 1) / c;
+    const size_t bytes = (size_t)per * mx * sizeof(cplx<T>);
+    // enough warps in the cluster for one column pair each per round
+    if (bytes <= limit && (c * warps >= pairs || c == 16)) {
+      *cs = c;
+      *cpc = per;
+      *smem = bytes;
+      return QCA_OK;
     }
   }
   return QCA_ERR_INVALID;
@@ -728,18 +679,17 @@ int svd_cluster_plan(int mx, int nx, int* cs, int* cpc, size_t* smem, int* v_sme
 template <typename T>
 int svd_cluster_size(int Dl, int Dr, int right_sweep) {
   const int p = right_sweep ? 2 * Dr : 2 * Dl, mx = right_sweep ? 2 * Dl : 2 * Dr, nx = p < mx ? p : mx;
-  int cs, cpc, vs;
+  int cs, cpc;
   size_t sm;
-  if (svd_block_plan<T>(mx, nx, &cs, &cpc, &sm, &vs)) return cs;
-  if (svd_cluster_plan<T>(mx, nx, &cs, &cpc, &sm, &vs) != QCA_OK) return 0;
+  if (svd_block_plan<T>(mx, nx, &cs, &cpc, &sm)) return cs;
+  if (svd_cluster_plan<T>(mx, nx, &cs, &cpc, &sm) != QCA_OK) return 0;
   return cs;
 }
 
-template <typename T>
-static int launch_cluster(void (*kern)(const SvdDesc<T>*, int, int, int), const SvdDesc<T>* d, int nd, int cs,
-                          int a1, int a2, size_t smem, cudaStream_t st) {
+template <typename... Args>
+static int launch_clustered(void (*kern)(Args...), int ctas, int cs, size_t smem, cudaStream_t st, Args... args) {
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(nd * cs, 1, 1);
+  cfg.gridDim = dim3(ctas, 1, 1);
   cfg.blockDim = dim3(kSvdThreads, 1, 1);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
@@ -750,16 +700,7 @@ static int launch_cluster(void (*kern)(const SvdDesc<T>*, int, int, int), const 
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  QCA_CUDA(cudaLaunchKernelEx(&cfg, kern, d, cs, a1, a2));
-  return QCA_OK;
-}
-
-template <typename T>
-static int configure(void (*kern)(const SvdDesc<T>*, int, int, int), bool* done) {
-  if (*done) return QCA_OK;
-  QCA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSvdSmem));
-  QCA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-  *done = true;
+  QCA_CUDA(cudaLaunchKernelEx(&cfg, kern, args...));
   return QCA_OK;
 }
 
@@ -768,7 +709,7 @@ int launch_svd(const SvdDesc<T>* d, const SvdDesc<T>* h, int nd, cudaStream_t st
   if (nd <= 0) return QCA_OK;
   int mxmax = 1, nxmax = 1;
   for (int i = 0; i < nd; ++i) {
-    // Jacobi runs on X = R^H: q rows (2 Dr right, 2 Dl left), K = min(p, q) columns
+    // Jacobi runs on X = R^H: q rows (2 Dl right, 2 Dr left), K = min(p, q) columns
     const int p = h[i].right_sweep ? 2 * h[i].Dr : 2 * h[i].Dl, q = h[i].right_sweep ? 2 * h[i].Dl : 2 * h[i].Dr;
     mxmax = std::max(mxmax, q);
     nxmax = std::max(nxmax, std::min(p, q));
@@ -780,47 +721,36 @@ int launch_svd(const SvdDesc<T>* d, const SvdDesc<T>* h, int nd, cudaStream_t st
   }
   const int rpl = rows <= 2 ? 2 : rows <= 4 ? 4 : rows <= 8 ? 8 : 16;
   const int ti = sizeof(T) == 8 ? 0 : 1, ri = rpl == 2 ? 0 : rpl == 4 ? 1 : rpl == 8 ? 2 : 3;
-  int P = 1, b = 1, vs = 1;
+  const int dv = device_slot();
+  int P = 1, b = 1;
   size_t smem = 0;
-  if (svd_block_plan<T>(mxmax, nxmax, &P, &b, &smem, &vs)) {
+  if (svd_block_plan<T>(mxmax, nxmax, &P, &b, &smem)) {
     // column length <= 256: RPL <= 8
     static bool configured[kMaxDevices][2][3] = {};
-    const int dv = device_slot();
-    void (*kern)(const SvdDesc<T>*, int, int) =
+    void (*kern)(const SvdDesc<T>*, int) =
         rpl == 2 ? svd_block_kernel<T, 2> : rpl == 4 ? svd_block_kernel<T, 4> : svd_block_kernel<T, 8>;
     if (dv < 0 || !configured[dv][ti][ri]) {
       QCA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSvdSmem));
       QCA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
       if (dv >= 0) configured[dv][ti][ri] = true;
     }
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(nd * P, 1, 1);
-    cfg.blockDim = dim3(kSvdThreads, 1, 1);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = P;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    QCA_CUDA(cudaLaunchKernelEx(&cfg, kern, d, P, vs));
-    return QCA_OK;
+    return launch_clustered(kern, nd * P, P, smem, st, d, P);
   }
   int cs = 1, cpc = 1;
-  if (svd_cluster_plan<T>(mxmax, nxmax, &cs, &cpc, &smem, &vs) != QCA_OK) {
+  if (svd_cluster_plan<T>(mxmax, nxmax, &cs, &cpc, &smem) != QCA_OK) {
     set_error("SVD of %d x %d exceeds the distributed shared memory of a 16-CTA cluster", mxmax, nxmax);
     return QCA_ERR_INVALID;
   }
   static bool configured[kMaxDevices][2][4] = {};
-  const int dv = device_slot();
-  bool once = false;
-  void (*kern)(const SvdDesc<T>*, int, int, int) =
+  void (*kern)(const SvdDesc<T>*, int, int) =
       rpl == 2 ? svd_cluster_kernel<T, 2>
                : rpl == 4 ? svd_cluster_kernel<T, 4> : rpl == 8 ? svd_cluster_kernel<T, 8> : svd_cluster_kernel<T, 16>;
-  QCA_TRY(configure<T>(kern, dv >= 0 ? &configured[dv][ti][ri] : &once));
-  return launch_cluster<T>(kern, d, nd, cs, cpc, vs, smem, st);
+  if (dv < 0 || !configured[dv][ti][ri]) {
+    QCA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSvdSmem));
+    QCA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    if (dv >= 0) configured[dv][ti][ri] = true;
+  }
+  return launch_clustered(kern, nd * cs, cs, smem, st, d, cs, cpc);
 }
 
 template int launch_svd<double>(const SvdDesc<double>*, const SvdDesc<double>*, int, cudaStream_t);
@@ -841,23 +771,20 @@ static int test_svd(int Dl, int Dr, const void* theta, int chi, double eps, int 
   using namespace qca;
   const int p = 2 * Dr, q = 2 * Dl, K = std::min(p, q);  // right sweep: W = Theta^H
   const size_t es = sizeof(cplx<T>);
-  // scratch: QR work (p q + p K), tau (K), Q (p K), R (K q), V (K^2), flags, descriptors
-  const size_t n_work = (size_t)p * q + (size_t)p * K, n_tau = K, n_q = (size_t)p * K, n_r = (size_t)K * q,
-               n_v = (size_t)K * K;
-  const size_t elems = n_work + n_tau + n_q + n_r + n_v;
+  // scratch: QR work (p q + p K), tau (K), R (K q), flags, descriptors
+  const size_t n_work = (size_t)p * q + (size_t)p * K, n_tau = K, n_r = (size_t)K * q;
+  const size_t elems = n_work + n_tau + n_r;
   const size_t fbytes = 64, dbytes = 2 * ((sizeof(SvdDesc<T>) + 63) / 64) * 64 + 2 * ((sizeof(QrDesc<T>) + 63) / 64) * 64;
   void* scratch = nullptr;
   QCA_CUDA(cudaMalloc(&scratch, elems * es + fbytes + dbytes));
   cplx<T>* base = (cplx<T>*)scratch;
   cplx<T>* work = base;
   cplx<T>* tau = work + n_work;
-  cplx<T>* Q = tau + n_tau;
-  cplx<T>* R = Q + n_q;
-  cplx<T>* Vw = R + n_r;
+  cplx<T>* R = tau + n_tau;
   char* flags = (char*)(base + elems);
   SvdDesc<T>* dd = (SvdDesc<T>*)(flags + fbytes);
   QrDesc<T>* dq = (QrDesc<T>*)((char*)dd + ((sizeof(SvdDesc<T>) + 63) / 64) * 64);
-  const QrDesc<T> qd = split_qr_desc<T>((const cplx<T>*)theta, Dl, Dr, 1, work, tau, Q, R);
+  const QrDesc<T> qd = split_qr_desc<T>((const cplx<T>*)theta, Dl, Dr, 1, work, tau, R);
   SvdDesc<T> d;
   memset(&d, 0, sizeof(d));
   d.theta = (const cplx<T>*)theta;
@@ -870,9 +797,7 @@ static int test_svd(int Dl, int Dr, const void* theta, int chi, double eps, int 
   d.max_sweeps = max_sweeps;
   d.Al = (cplx<T>*)Al;
   d.Ar = (cplx<T>*)Ar;
-  d.qmat = Q;
   d.rmat = R;
-  d.work = Vw;
   d.sv = sv;
   d.k_out = (int*)flags;
   d.status = (int*)(flags + 16);

@@ -142,10 +142,10 @@ int launch_lz_combine(const LanczosDesc<T>* d, const LanczosDesc<T>* h, int nd, 
 // min(p, q)), and one-sided Jacobi runs on X = R^H (q x K), whose columns are
 // graded and nearly orthogonal, so the sweeps converge in a few rounds instead of
 // the dozens the raw, strongly graded two-site matrix needs.  With X (rotated)
-// orthogonal: W^H = (X / Sigma) Sigma (Q V)^H, so the factor the sweep needs
-// isometric (A_l on a right sweep, A_r on a left one) is X / Sigma, whose
+// orthogonal: W^H = U Sigma (Q V)^H with U = X / Sigma, so the factor the sweep
+// needs isometric (A_l on a right sweep, A_r on a left one) is U, whose
 // orthogonality the Jacobi tolerance enforces directly, and the other factor is
-// (Q V) Sigma, which carries the rounding of the accumulated rotations V.
+// W U: Q and the rotations V are never formed.
 template <typename T>
 struct SvdDesc {
   const cplx<T>* theta;  // theta[s][a][c], s = s1*2+s2, dims (4, Dl, Dr)
@@ -156,9 +156,7 @@ struct SvdDesc {
   int right_sweep;       // 1: A_l = U, A_r = s Vh ; 0: A_l = U s, A_r = Vh
   cplx<T>* Al;           // out (2, Dl, k)
   cplx<T>* Ar;           // out (2, k, Dr)
-  const cplx<T>* qmat;   // Q of W = Q R, column major p x K (p = 2 Dr right, 2 Dl left)
-  const cplx<T>* rmat;   // R, row major K x q (q = 2 Dl right, 2 Dr left)
-  cplx<T>* work;         // V columns when they do not fit in the cluster's shared memory (K^2)
+  const cplx<T>* rmat;   // R of W = Q R, row major K x q (q = 2 Dl right, 2 Dr left)
   double* sv;            // singular values (n_x), FP64
   int* k_out;            // new bond dimension
   double* discarded;     // discarded weight accumulator (+= sum of dropped s^2 / sum s^2)
@@ -210,11 +208,11 @@ int launch_qr(const QrDesc<T>* d, int nd, int gauge, cudaStream_t st);
 
 // The QR that preconditions a two-site split (see SvdDesc): W = Theta^H (right
 // sweep, p = 2 Dr, q = 2 Dl) or Theta (left sweep, p = 2 Dl, q = 2 Dr) read
-// straight from theta[s1*2+s2][a][c]; Q into q_out (column major p x K), R into
-// r_out (row major K x q).  work needs p q + p K elements, tau K.
+// straight from theta[s1*2+s2][a][c]; R into r_out (row major K x q); Q is not
+// formed.  work needs p q + p K elements, tau K.
 template <typename T>
 QrDesc<T> split_qr_desc(const cplx<T>* theta, int Dl, int Dr, int right_sweep, cplx<T>* work, cplx<T>* tau,
-                        cplx<T>* q_out, cplx<T>* r_out) {
+                        cplx<T>* r_out) {
   QrDesc<T> d;
   memset(&d, 0, sizeof(d));
   const long long blk = (long long)Dl * Dr;
@@ -241,12 +239,7 @@ QrDesc<T> split_qr_desc(const cplx<T>* theta, int Dl, int Dr, int right_sweep, c
   d.complete = 0;
   d.work = work;
   d.tau = tau;
-  d.q = q_out;
-  d.qsplit = p;
-  d.sQr0 = 1;
-  d.sQc = p;
-  d.qrows_out = p;
-  d.qcols_out = K;
+  d.q = nullptr;
   d.rr = r_out;
   d.sRr = q;
   d.sRc = 1;
