@@ -42,6 +42,8 @@ extern "C" {
 /* ---- algorithms (parameters/parser.py:75-82) -------------------------------- */
 #define QCA_ALGO_1TDVP 1
 #define QCA_ALGO_2TDVP 2
+#define QCA_ALGO_A1TDVP 3 /* 1TDVP whose target bond dimensions are recomputed before every
+                             step from 2-site splits (tdvp.py:212-267) */
 
 const char* qca_last_error(void);
 int qca_version(void);
@@ -118,7 +120,7 @@ typedef struct qca_chain_desc {
   const int* mps_bonds;    /* N+1 MPS bond dimensions D_0..D_N (D_0 = D_N = 1)           */
   const double* mps;       /* A[0..N-1] concatenated; A[i] is (2,D_i,D_{i+1}) complex128
                               (tensor_networks/mps.py:14-25)                            */
-  int algorithm;           /* QCA_ALGO_1TDVP or QCA_ALGO_2TDVP (tdvp.py:55-63)           */
+  int algorithm;           /* QCA_ALGO_1TDVP, QCA_ALGO_2TDVP or QCA_ALGO_A1TDVP (tdvp.py:55-63) */
   int max_bond_dim;        /* --max-bond-dim (parameters/parser.py:106-113)             */
   double svd_epsilon;      /* --svd-epsilon (parameters/parser.py:114-122)              */
   double step_size;        /* dt; the local propagator is exp(-i pi/2 dt/2 H_eff)        */

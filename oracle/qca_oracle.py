@@ -379,7 +379,7 @@ class TDVPOracle:
 
     def __init__(self, A: list[np.ndarray], W: list[np.ndarray], algorithm: str, step_size: float,
                  max_bond_dim: int, svd_epsilon: float, fixed: bool = True) -> None:
-        assert algorithm in ("1tdvp", "2tdvp")
+        assert algorithm in ("1tdvp", "2tdvp", "a1tdvp")
         self.A = [np.array(a, dtype=np.complex128) for a in A]
         self.W = W
         self.algorithm = algorithm
@@ -392,7 +392,8 @@ class TDVPOracle:
         make_site_canonical(self.A, 0)
         self.L: list = [None] * n
         self.R: list = [None] * n
-        self.target = [min(2 ** i, 2 ** (n - i), max_bond_dim) for i in range(n + 1)]
+        self.max_bonds = [min(2 ** i, 2 ** (n - i), max_bond_dim) for i in range(n + 1)]
+        self.target = list(self.max_bonds)
         for site in reversed(range(1, n)):
             make_site_canonical(self.A, site - 1)
             self._update_env("right", site)
@@ -475,8 +476,39 @@ class TDVPOracle:
             yield from self._sweep_right_2()
             yield from self._sweep_left_2()
         else:
+            if self.algorithm == "a1tdvp":
+                self._new_target_bond_dims()
             yield from self._sweep_right_1()
             yield from self._sweep_left_1()
+
+    def _new_target_bond_dims(self) -> None:
+        """``tdvp.py:212-267`` (``a1tdvp``): the target bond dimensions of the next
+        1TDVP step.  Left-canonical sweep with left environments; then, bond by bond
+        from the right, the two-site tensor evolved by dt/2 (the reference's
+        ``exact_exponential`` method, i.e. the local exponential of every other
+        update) is split and the bond's target set to min{i : ||s[i:]|| < eps}
+        (else the maximal bond dimension), clamped to [1, maximal]; the evolved
+        tensor itself is discarded.  ``fixed`` rebuilds each right environment after
+        the right gauge move, so that the next bond's effective Hamiltonian matches
+        the tensors; the reference keeps the environments of the previous sweep."""
+        n = len(self.A)
+        for site in range(n - 1):
+            make_site_canonical(self.A, site + 1)
+            self._update_env("left", site)
+        for bond in reversed(range(1, n)):
+            Al, Ar = self.A[bond - 1], self.A[bond]
+            sl, sr = Al.shape, Ar.shape
+            th = np.tensordot(Al, Ar, (2, 1)).transpose(0, 2, 1, 3).reshape(sl[0] * sr[0], sl[1], sr[2])
+            th = self._local_exp(self._env("left", bond - 2), self._env("right", bond + 1),
+                                 _merge_w(self.W[bond - 1], self.W[bond]), th, self.dt / 2)
+            th = th.reshape(sl[0], sr[0], sl[1], sr[2]).transpose(0, 2, 1, 3).reshape(sl[0] * sl[1], sr[0] * sr[2])
+            s = np.linalg.svd(th, compute_uv=False)
+            cap = min(self.max_bonds[bond], len(s))
+            new = next((i for i in range(len(s)) if np.linalg.norm(s[i:]) < self.eps), cap)
+            self.target[bond] = max(1, min(new, cap))
+            make_site_canonical(self.A, bond - 1)
+            if self.fixed:
+                self._update_env("right", bond)
 
     def _sweep_right_2(self):
         n = len(self.A)

@@ -26,6 +26,7 @@ QCA_PREC_FP64 = 0
 QCA_PREC_MIXED = 1
 QCA_ALGO_1TDVP = 1
 QCA_ALGO_2TDVP = 2
+QCA_ALGO_A1TDVP = 3
 
 _ERROR_NAMES = {
     QCA_ERR_INVALID: "invalid argument",

@@ -176,7 +176,7 @@ def chain_desc(A: list, W: list, algorithm: str, step_size: float, max_bond_dim:
     n = len(A)
     if len(W) != n:
         raise ValueError("MPO and MPS lengths differ")
-    if algorithm not in ("1tdvp", "2tdvp"):
+    if algorithm not in ("1tdvp", "2tdvp", "a1tdvp"):
         raise ValueError(f"algorithm {algorithm!r} is not a TDVP variant handled here")
     mps_bonds = np.array([a.shape[1] for a in A] + [A[-1].shape[2]], dtype=np.int32)
     mpo_bonds = np.array([w.shape[2] for w in W] + [W[-1].shape[3]], dtype=np.int32)
@@ -188,7 +188,8 @@ def chain_desc(A: list, W: list, algorithm: str, step_size: float, max_bond_dim:
     d.mpo = mpo.ctypes.data_as(_lib._PD)
     d.mps_bonds = mps_bonds.ctypes.data_as(_lib._PI)
     d.mps = mps.ctypes.data_as(_lib._PD)
-    d.algorithm = _lib.QCA_ALGO_1TDVP if algorithm == "1tdvp" else _lib.QCA_ALGO_2TDVP
+    d.algorithm = {"1tdvp": _lib.QCA_ALGO_1TDVP, "2tdvp": _lib.QCA_ALGO_2TDVP,
+                   "a1tdvp": _lib.QCA_ALGO_A1TDVP}[algorithm]
     d.max_bond_dim = int(max_bond_dim)
     d.svd_epsilon = float(svd_epsilon)
     d.step_size = float(step_size)
@@ -210,6 +211,9 @@ class GpuTDVP(Algorithm):
 
     The 2-site variant is the gauge-consistent form of the reference (right
     environments consistent with the tensors at the start of every sweep).
+    ``a1tdvp`` is 1TDVP whose target bond dimensions are recomputed before every
+    step from evolved two-site splits (``tdvp.py:212-267``, with the exact local
+    exponential of the reference's ``exact_exponential`` method).
     """
 
     def __init__(self, psi_0, H, args, stream=None, engine: _Engine | None = None) -> None:
@@ -289,6 +293,6 @@ def algorithm_class(name: str):
     """``quantum_game.py:62-68``: the class for an ``--algorithm`` string."""
     if name == "exact":
         return GpuExact
-    if name in ("1tdvp", "2tdvp"):
+    if name in ("1tdvp", "2tdvp", "a1tdvp"):
         return GpuTDVP
     raise ValueError(f"algorithm {name!r} is not provided by the GPU path")

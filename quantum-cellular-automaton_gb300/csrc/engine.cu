@@ -131,6 +131,8 @@ struct Chain {
   int N = 0, algo = 0, chi = 0;
   double eps = 0, dt = 0;
   std::vector<int> w, D, cap, target;
+  std::vector<int> maxb;  // min(2^i, 2^(N-i), chi) (tdvp.py:31-35); target is recomputed by a1tdvp
+  int* a1flags = nullptr; // a1tdvp pass: [b] new target of bond b, [N + 1 + 2 b] SVD status, [+1] sweeps
   std::vector<cplx<T>*> A[2];
   std::vector<int> par;
   std::vector<cplx<T>*> Lenv, Renv;  // Lenv[i+1]: after site i (Lenv[0] = boundary); Renv[i]: before site i
@@ -1235,7 +1237,7 @@ struct Engine final : EngineBase {
     std::vector<int> dold(C.size(), 0);
     for (size_t ci = 0; ci < C.size(); ++ci) {
       Chain<T>* c = C[ci];
-      if (c->algo != QCA_ALGO_1TDVP) continue;
+      if (c->algo == QCA_ALGO_2TDVP) continue;
       const int s = c->pos;
       if (c->dir == 0 && s < c->N - 1) {
         dold[ci] = c->D[s + 1];
@@ -1292,7 +1294,7 @@ struct Engine final : EngineBase {
     std::vector<std::pair<Chain<T>*, int>> flips;
     for (size_t ci = 0; ci < C.size(); ++ci) {
       Chain<T>* c = C[ci];
-      if (c->algo != QCA_ALGO_1TDVP) continue;
+      if (c->algo == QCA_ALGO_2TDVP) continue;
       const int s = c->pos;
       if (c->dir == 0 && s < c->N - 1) {
         const int tg = c->D[s + 1], Do = dold[ci], Dk = c->D[s + 2];
@@ -1479,6 +1481,119 @@ struct Engine final : EngineBase {
       QCA_CUDA(cudaMemsetAsync(c->iflags + 3, 0, sizeof(int), st));
     }
     if (!dirty.empty()) QCA_TRY(canonicalize_right(dirty, false, st));
+    std::vector<Chain<T>*> a1;
+    for (auto* c : starting)
+      if (c->algo == QCA_ALGO_A1TDVP) a1.push_back(c);
+    if (!a1.empty()) QCA_TRY(a1_targets(a1, st));
+    return QCA_OK;
+  }
+
+  // a1tdvp (tdvp.py:212-267): the target bond dimensions of the coming 1TDVP step,
+  // for every listed chain in lock step.  A left-canonical sweep with left
+  // environments (make_site_canonical(site + 1) and the left layer, tdvp.py:
+  // 214-216), then bond by bond from the right end: the two-site tensor evolved by
+  // dt/2 with the current environments (the right ones as the previous step left
+  // them, as in the reference), its split's truncation rule (first i with
+  // ||s[i:]|| < eps, else the maximal bond; clamped to [1, maximal]) as the bond's
+  // target, the evolved tensor discarded, and a right gauge move
+  // (make_site_canonical(bond - 1)).  The SVDs write their truncated dimension to
+  // a per-chain device array read once at the end.
+  int a1_targets(std::vector<Chain<T>*>& C, cudaStream_t st) {
+    const double hp = M_PI / 2;
+    int maxN = 0;
+    for (auto* c : C) {
+      maxN = std::max(maxN, c->N);
+      QCA_CUDA(cudaMemsetAsync(c->a1flags, 0, sizeof(int) * 3 * (c->N + 1), st));
+    }
+    for (int site = 0; site + 1 < maxN; ++site) {
+      std::vector<MoveJob> J;
+      std::vector<EnvJob> E;
+      for (auto* c : C)
+        if (site < c->N - 1) {
+          J.push_back(MoveJob{c, site, true});
+          E.push_back(EnvJob{c, site, true});
+        }
+      QCA_TRY(qr_moves(J, st));
+      QCA_TRY(env_update(E, st));
+    }
+    for (int t = 0; t + 1 < maxN; ++t) {  // bond N-1-t of every chain
+      std::vector<GemmDesc<T>> form;
+      std::vector<LzProb> P;
+      std::vector<SvdDesc<T>> sv;
+      std::vector<QrDesc<T>> spre;
+      std::vector<MoveJob> J;
+      for (auto* c : C) {
+        const int bond = c->N - 1 - t;
+        if (bond < 1) continue;
+        const int l = bond - 1, r = bond;
+        const int Dl = c->D[l], Dm = c->D[l + 1], Dr = c->D[r + 1];
+        GemmDesc<T> g = gemm0();
+        g.A = c->cur(l);
+        g.B = c->cur(r);
+        g.C = c->theta;
+        g.M = Dl;
+        g.K = Dm;
+        g.N = Dr;
+        g.nb1 = 2;
+        g.nb2 = 2;
+        g.sAm = Dm;
+        g.sAk = 1;
+        g.sAb1 = (long long)Dl * Dm;
+        g.sBk = Dr;
+        g.sBn = 1;
+        g.sBb2 = (long long)Dm * Dr;
+        g.sCm = Dr;
+        g.sCn = 1;
+        g.sCb1 = 2LL * Dl * Dr;
+        g.sCb2 = (long long)Dl * Dr;
+        form.push_back(g);
+        P.push_back(LzProb{c, 4, Dl, Dr, c->w[l], c->w[r + 1], c->Lenv[l], c->Renv[r + 1], c->mv2[l], c->theta,
+                           c->theta, hp * c->dt / 2});
+        SvdDesc<T> d;
+        memset(&d, 0, sizeof(d));
+        d.theta = c->theta;
+        d.Dl = Dl;
+        d.Dr = Dr;
+        d.chi = c->maxb[bond];
+        d.kmax = c->cap[bond];
+        d.eps = c->eps;
+        d.right_sweep = 1;
+        d.Al = c->t1;  // the split itself is discarded
+        d.Ar = c->t2;
+        d.rmat = c->svdw;
+        d.sv = c->sv;
+        d.k_out = c->a1flags + bond;
+        d.discarded = c->dscal + 1;
+        d.status = c->a1flags + c->N + 1 + 2 * bond;
+        sv.push_back(d);
+        spre.push_back(split_qr_desc<T>(c->theta, Dl, Dr, 1, c->qrw, c->qrtau, c->svdw));
+        J.push_back(MoveJob{c, bond, false});
+      }
+      QCA_TRY(run_gemm(form, st));
+      QCA_TRY(lanczos(P, st));
+      QCA_TRY(check_svd(sv));
+      QCA_TRY(check_qr(spre));
+      const QrDesc<T>* dq;
+      QCA_TRY(upload(spre, st, &dq));
+      QCA_TRY(timed(KC_SVD, 0, 0, st, [&] { return launch_qr<T>(dq, (int)spre.size(), 1, st); }));
+      QCA_TRY(timed(KC_SVD, 0, 0, st, [&] { return svd_grouped(sv, st); }));
+      QCA_TRY(qr_moves(J, st));
+    }
+    for (auto* c : C) {
+      std::vector<int> h(3 * (c->N + 1));
+      QCA_CUDA(cudaMemcpyAsync(h.data(), c->a1flags, sizeof(int) * h.size(), cudaMemcpyDeviceToHost, st));
+      QCA_TRY(sync(st));
+      for (int b = 1; b < c->N; ++b) {
+        const int k = h[b];
+        if (k < 1 || k > c->cap[b]) {
+          set_error("a1tdvp: split returned bond dimension %d (capacity %d)", k, c->cap[b]);
+          return QCA_ERR_INVALID;
+        }
+        c->target[b] = k;
+        note_failure(c, h[c->N + 1 + 2 * b], 0, b);
+      }
+      c->center = 0;
+    }
     return QCA_OK;
   }
 
@@ -1877,6 +1992,7 @@ static void plan_chain(const qca_chain_desc* d, int mmax, Layout& Lo, std::vecto
   put(sizeof(double) * 4 * cmax);           // singular values
   put(sizeof(double) * (8 + 4 * N));        // discarded weight + rho
   put(sizeof(int) * 8);                     // flags
+  put(sizeof(int) * 3 * (N + 1));           // a1tdvp targets and SVD statuses
   if (nmax_out) *nmax_out = nmax;
   if (tmax_out) *tmax_out = tmax;
   if (cmax_out) *cmax_out = cmax;
@@ -1887,7 +2003,8 @@ template <typename T>
 int Engine<T>::add(const qca_chain_desc* d, cudaStream_t st, int* id_out) {
   const int N = d->n_sites;
   if (N < 2 || !d->mpo_bonds || !d->mpo || !d->mps_bonds || !d->mps || d->max_bond_dim < 1 ||
-      (d->algorithm != QCA_ALGO_1TDVP && d->algorithm != QCA_ALGO_2TDVP) || !(d->svd_epsilon >= 0) ||
+      (d->algorithm != QCA_ALGO_1TDVP && d->algorithm != QCA_ALGO_2TDVP && d->algorithm != QCA_ALGO_A1TDVP) ||
+      !(d->svd_epsilon >= 0) ||
       !std::isfinite(d->step_size)) {
     set_error("qca_chain_add: invalid chain description");
     return QCA_ERR_INVALID;
@@ -1961,6 +2078,7 @@ int Engine<T>::add(const qca_chain_desc* d, cudaStream_t st, int* id_out) {
     if (i < 40) t = std::min<long long>(t, 1LL << i);
     if (N - i < 40) t = std::min<long long>(t, 1LL << (N - i));
     c->target[i] = (int)t;
+    c->maxb.push_back((int)t);
   }
   c->nmax = nmax;
   c->max_chunks = chunks;
@@ -1990,6 +2108,7 @@ int Engine<T>::add(const qca_chain_desc* d, cudaStream_t st, int* id_out) {
   c->sv = (double*)(base + offs[k++]);
   c->dscal = (double*)(base + offs[k++]);
   c->iflags = (int*)(base + offs[k++]);
+  c->a1flags = (int*)(base + offs[k++]);
   // entry lists: laid out back to back at the end of the allocation, uploaded as
   // one host image
   std::vector<EL> els;

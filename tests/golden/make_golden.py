@@ -16,6 +16,7 @@ Fixtures:
   qr_lapack.npz        numpy.linalg.qr outputs (complete and reduced) incl.
                        zero-padded and rank-deficient inputs
   measure_case.npz     MPS.measure outputs for a random MPS and a product state
+  a1tdvp_series.npz    a1tdvp populations / bond dims (exact_exponential local evolution)
 """
 from __future__ import annotations
 
@@ -144,6 +145,43 @@ def gen_tdvp(ref):
     np.savez_compressed(os.path.join(HERE, "tdvp_series.npz"), **out)
 
 
+A1TDVP_CASES = [
+    # name, n, d, lo, hi, p (None = random seed 13), dt, chi, eps, steps
+    ("a1_single8", 8, 1, 1, 2, [0.0] * 3 + [1.0] + [0.0] * 4, 0.1, 8, 1e-3, 6),
+    ("a1_rand8", 8, 2, 2, 4, None, 0.05, 8, 1e-4, 5),
+]
+
+
+def gen_a1tdvp(ref):
+    """The reference's a1tdvp (tdvp.py:212-267) with its "exact_exponential" local
+    evolution (the default "taylor" path calls np.math, absent from numpy 2):
+    populations and bond dimensions after every step, measured like the driver."""
+    out = {}
+    for name, n, d, lo, hi, p, dt, chi, eps, steps in A1TDVP_CASES:
+        if p is None:
+            th = np.random.default_rng(13).uniform(0, np.pi / 2, size=n)
+            p = list(np.sin(th) ** 2)
+        r = ref.Rules(ncells=n, activation_interval=range(lo, hi), distance=d, periodic=False)
+        H = ref.MPO.hamiltonian_from_rules(r)
+        psi0 = ref.MPS.from_density_distribution(p)
+        args = types.SimpleNamespace(step_size=dt, algorithm="a1tdvp", max_bond_dim=chi, svd_epsilon=eps,
+                                     approximative_evolution_method="exact_exponential", taylor_steps=10)
+        alg = ref.TDVP(psi_0=psi0, H=H, args=args)
+        pops = np.zeros((steps + 1, n))
+        dpop = np.zeros((steps + 1, n))
+        sse = np.zeros((steps + 1, n))
+        bonds = np.zeros((steps + 1, n + 1))
+        for s_ in range(steps + 1):
+            alg.measure(pops[s_], dpop[s_], sse[s_], bonds[s_])
+            if s_ < steps:
+                alg.do_time_step()
+        out[f"{name}_ref_pop"] = pops
+        out[f"{name}_ref_bonds"] = bonds
+        out[name + "_p"] = np.array(p)
+        out[name + "_meta"] = np.array([n, d, lo, hi, dt, chi, eps, steps])
+    np.savez_compressed(os.path.join(HERE, "a1tdvp_series.npz"), **out)
+
+
 def gen_qr():
     rng = np.random.default_rng(3)
     out = {}
@@ -183,15 +221,17 @@ def gen_measure(ref):
     np.savez_compressed(os.path.join(HERE, "measure_case.npz"), **out)
 
 
+GENERATORS = {"mpo": gen_mpo, "exact": gen_exact, "tdvp": gen_tdvp, "a1tdvp": gen_a1tdvp,
+              "qr": lambda ref: gen_qr(), "measure": gen_measure}
+
+
 def main() -> None:
-    if len(sys.argv) != 2:
-        sys.exit("usage: python tests/golden/make_golden.py <path of the reference checkout>")
+    if len(sys.argv) < 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the reference checkout> [fixture ...]\n"
+                 "fixtures: " + " ".join(GENERATORS) + " (default: all)")
     ref = load_reference(sys.argv[1])
-    gen_mpo(ref)
-    gen_exact(ref)
-    gen_tdvp(ref)
-    gen_qr()
-    gen_measure(ref)
+    for name in sys.argv[2:] or list(GENERATORS):
+        GENERATORS[name](ref)
     print("golden fixtures written to", HERE)
 
 

@@ -172,3 +172,21 @@ def test_krylov_tdvp_oracle_matches_dense_oracle(alg):
         b.step()
         assert [x.shape for x in a.A] == [x.shape for x in b.A]
     assert np.abs(O.mps_as_vector(a.A) - O.mps_as_vector(b.A)).max() < 1e-10
+
+
+@pytest.mark.parametrize("name", ["a1_single8", "a1_rand8"])
+def test_oracle_a1tdvp_matches_reference(golden, name):
+    """The oracle's a1tdvp (tdvp.py:212-267, the reference's exact_exponential local
+    evolution, its environments as the reference keeps them) reproduces the
+    reference's populations and bond dimensions (fixture a1tdvp_series.npz)."""
+    t = golden("a1tdvp_series.npz")
+    n, d, lo, hi, dt, chi, eps, steps = t[name + "_meta"]
+    n, d, lo, hi, chi, steps = int(n), int(d), int(lo), int(hi), int(chi), int(steps)
+    orc = O.TDVPOracle(O.mps_from_density_distribution(t[name + "_p"]), O.build_mpo(O.Rules(n, range(lo, hi), d)),
+                       "a1tdvp", float(dt), chi, float(eps), fixed=False)
+    for s in range(steps + 1):
+        pop, _, _, bonds = O.measure(orc.A)
+        assert np.abs(pop - t[name + "_ref_pop"][s]).max() < 1e-12, s
+        assert np.array_equal(bonds, t[name + "_ref_bonds"][s]), s
+        if s < steps:
+            orc.step()

@@ -174,3 +174,22 @@ def test_tdvp_mixed_tracks_fp64_at_large_bonds(alg_name):
         res.append(r)
     assert np.abs(res[0][0] - res[1][0]).max() < (3e-5 if alg_name == "2tdvp" else TOL_MIXED_1TDVP)
 
+
+
+@pytest.mark.parametrize("name", ["a1_single8", "a1_rand8"])
+def test_a1tdvp_matches_reference(golden, name):
+    """a1tdvp (tdvp.py:212-267) on the GPU against the reference's own run (fixture
+    a1tdvp_series.npz, exact_exponential local evolution): populations within
+    1e-8 and identical bond dimensions after every step, with the reference's
+    measurements between the steps."""
+    t = golden("a1tdvp_series.npz")
+    n, d, lo, hi, dt, chi, eps, steps = t[name + "_meta"]
+    n, d, lo, hi, chi, steps = int(n), int(d), int(lo), int(hi), int(chi), int(steps)
+    alg = make("a1tdvp", n, d, lo, hi, t[name + "_p"], float(dt), chi, float(eps))
+    for s in range(steps + 1):
+        pop, dpop, sse, bonds = rows(n)
+        alg.measure(pop, dpop, sse, bonds)
+        assert np.abs(pop - t[name + "_ref_pop"][s]).max() < TOL_FP64, s
+        assert np.array_equal(bonds, t[name + "_ref_bonds"][s]), (s, bonds)
+        if s < steps:
+            alg.do_time_step()
