@@ -973,7 +973,7 @@ struct Engine final : EngineBase {
 
   // Right QR sweep to site 0 and rebuild of every right environment, in lock step
   // over the chains (make_site_canonical(0), mps.py:184-192, plus tdvp.py:37-39).
-  int canonicalize_right(std::vector<Chain<T>*>& C, bool from_init, cudaStream_t st) {
+  int canonicalize_right(std::vector<Chain<T>*>& C, bool rebuild_env, cudaStream_t st) {
     int maxN = 0;
     for (auto* c : C) maxN = std::max(maxN, c->N);
     // QR moves from the centre down to site 1
@@ -984,13 +984,12 @@ struct Engine final : EngineBase {
       QCA_TRY(qr_moves(J, st));
     }
     // right environments N-1 .. 1
-    for (int k = maxN - 1; k >= 1; --k) {
+    for (int k = maxN - 1; rebuild_env && k >= 1; --k) {
       std::vector<EnvJob> J;
       for (auto* c : C)
         if (k < c->N) J.push_back(EnvJob{c, k, false});
       QCA_TRY(env_update(J, st));
     }
-    (void)from_init;
     for (auto* c : C) c->center = 0;
     return QCA_OK;
   }
@@ -1480,7 +1479,13 @@ struct Engine final : EngineBase {
       QCA_CUDA(cudaMemsetAsync(c->dscal, 0, sizeof(double), st));
       QCA_CUDA(cudaMemsetAsync(c->iflags + 3, 0, sizeof(int), st));
     }
-    if (!dirty.empty()) QCA_TRY(canonicalize_right(dirty, false, st));
+    // the gauge-consistent start of 2TDVP and 1TDVP rebuilds the right environments
+    // after the re-canonicalisation; a1tdvp keeps those of the previous sweep, as
+    // the reference does (tdvp.py:54 and 212-267 read them as they are)
+    std::vector<Chain<T>*> dirty_env, dirty_keep;
+    for (auto* c : dirty) (c->algo == QCA_ALGO_A1TDVP ? dirty_keep : dirty_env).push_back(c);
+    if (!dirty_env.empty()) QCA_TRY(canonicalize_right(dirty_env, true, st));
+    if (!dirty_keep.empty()) QCA_TRY(canonicalize_right(dirty_keep, false, st));
     std::vector<Chain<T>*> a1;
     for (auto* c : starting)
       if (c->algo == QCA_ALGO_A1TDVP) a1.push_back(c);
