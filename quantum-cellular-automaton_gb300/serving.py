@@ -75,6 +75,8 @@ class Server:
         self.round_times: list[float] = []      # wall time of every scheduling round
         self.first_stream: list[float] = []     # arrival -> first streamed <n_i> per job
         self.max_overlap = 0                    # most jobs resident in one round
+        self.failures: dict[int, int] = {}      # status code -> jobs retired with it
+        self.first_failure: str | None = None   # the engine's message of the first failure
 
     # ------------------------------------------------------------------ requests
     def submit(self, spec: ChainSpec, arrival: float | None = None) -> int:
@@ -162,12 +164,15 @@ class Server:
         except _lib.QcaError as e:
             if e.code not in (_lib.QCA_ERR_NAN, _lib.QCA_ERR_NOT_CONVERGED):
                 raise
+            if self.first_failure is None:
+                self.first_failure = str(e)
         due, still = [], []
         t = time.perf_counter()
         for j in self.active:
             done, inside, status = self._progress(j)
             if status:
                 j.error = f"status {status}"
+                self.failures[status] = self.failures.get(status, 0) + 1
                 self._retire(j, t, failed=True)
                 continue
             if not inside and done >= j.scheduled_to and done > j.steps_done:
@@ -242,7 +247,9 @@ class Server:
         def pct(a, q):
             return float(np.percentile(a, q)) if a.size else None
 
-        return {"jobs_done": len(self.done), "jobs_failed": len(self.failed), "jobs_pending": len(self.pending),
+        return {"jobs_done": len(self.done), "jobs_failed": len(self.failed),
+                "failures_by_status": {str(k): v for k, v in self.failures.items()},
+                "first_failure": self.first_failure, "jobs_pending": len(self.pending),
                 "jobs_active": len(self.active), "max_resident": self.max_overlap,
                 "site_updates": self.site_updates, "elapsed_s": elapsed,
                 "site_updates_per_s": self.site_updates / elapsed if elapsed > 0 else 0.0,
