@@ -714,7 +714,8 @@ def run_serving(args, dist: Dist):
     def summary(r):
         return {"site_updates_per_s": round(r["site_updates_per_s"], 1), "jobs_done": r["jobs_done"],
                 "jobs_failed": r["jobs_failed"], "failures_by_status": r["failures_by_status"],
-                "first_failure": r["first_failure"], "jobs_unfinished": r["jobs_active"] + r["jobs_pending"],
+                "first_failure": r["first_failure"], "failed_jobs": r["failed_jobs"][:16],
+                "jobs_unfinished": r["jobs_active"] + r["jobs_pending"],
                 "p50_latency_s": r["p50_latency_s"], "p99_latency_s": r["p99_latency_s"],
                 "p50_first_populations_s": r["p50_first_stream_s"],
                 "p99_first_populations_s": r["p99_first_stream_s"], "max_resident_jobs": r["max_resident"],

@@ -2069,6 +2069,10 @@ int Engine<T>::add(const qca_chain_desc* d, cudaStream_t st, int* id_out) {
   }
   c->bytes = Lo.total;
   char* base = (char*)c->mem;
+  // A fresh chain starts from zeros, not from whatever a removed chain left in the
+  // recycled memory: zero padding then multiplies as zero (a stale NaN would not),
+  // and a chain's arithmetic cannot depend on the chains that came before it.
+  QCA_CUDA(cudaMemsetAsync(base, 0, Lo.total, st));
   c->N = N;
   c->algo = d->algorithm;
   c->chi = d->max_bond_dim;

@@ -63,7 +63,10 @@ __global__ void __launch_bounds__(kQrThreads) qr_kernel(const QrDesc<T>* __restr
       tr = (beta - ar) / beta;
       ti = -ai / beta;
       const cplx<double> den = mk<double>(ar - beta, ai);
-      if (sizeof(Acc) == 8) {
+      // |x_i / (alpha - beta)| <= 1 always, but the reciprocal of alpha - beta
+      // leaves the FP32 range for columns below ~1e-38 (denormal rounding residue):
+      // those divide element by element in FP64 instead of turning into inf * 0.
+      if (sizeof(Acc) == 8 || bnorm < 1e-30) {
         for (int i = k + 1 + threadIdx.x; i < m; i += blockDim.x) {
           const cplx<T> x = col[i];
           col[i] = cdiv<T>(mk<double>((double)x.re, (double)x.im), den);

@@ -123,6 +123,16 @@ class Server:
         _lib.call("qca_chain_progress", self.engine.h, js.chain, pr)
         return int(pr[0]), bool(pr[2]), int(pr[3])
 
+    def _failure_message(self, js: JobState, status: int) -> str:
+        """The engine's account of a failed chain (what failed, at which site): a
+        step request on a failed chain returns its recorded error without running."""
+        ids = (ctypes.c_int * 1)(js.chain)
+        try:
+            _lib.call("qca_engine_step_chains", self.engine.h, ids, 1, 1, None)
+        except _lib.QcaError as e:
+            return str(e)
+        return f"status {status}"
+
     def _measure(self, jobs: list[JobState]) -> None:
         if not jobs:
             return
@@ -171,7 +181,7 @@ class Server:
         for j in self.active:
             done, inside, status = self._progress(j)
             if status:
-                j.error = f"status {status}"
+                j.error = self._failure_message(j, status)
                 self.failures[status] = self.failures.get(status, 0) + 1
                 self._retire(j, t, failed=True)
                 continue
@@ -249,7 +259,11 @@ class Server:
 
         return {"jobs_done": len(self.done), "jobs_failed": len(self.failed),
                 "failures_by_status": {str(k): v for k, v in self.failures.items()},
-                "first_failure": self.first_failure, "jobs_pending": len(self.pending),
+                "first_failure": self.first_failure,
+                "failed_jobs": [{"job": j.job_id, "algorithm": j.spec.algorithm, "n": j.spec.n,
+                                 "distance": j.spec.distance, "chi": j.spec.chi, "steps_done": j.steps_done,
+                                 "error": j.error} for j in self.failed],
+                "jobs_pending": len(self.pending),
                 "jobs_active": len(self.active), "max_resident": self.max_overlap,
                 "site_updates": self.site_updates, "elapsed_s": elapsed,
                 "site_updates_per_s": self.site_updates / elapsed if elapsed > 0 else 0.0,
