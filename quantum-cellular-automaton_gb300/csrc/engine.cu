@@ -20,6 +20,8 @@
 //    including the canonicalisation after a measurement, because its bond
 //    growth uses the complement columns of the complete QR (tdvp.py:74, 95).
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <cmath>
 #include <limits>
 #include <map>
@@ -417,6 +419,29 @@ struct Engine final : EngineBase {
     });
     tile(big, kUmmaBM, kUmmaBN);
     tile(small, 64, 64);
+    if (!big.empty()) {
+      // QCA_UMMA_LOG=<file>: one line per tcgen05 launch (its ordinal among this
+      // process's tcgen05 launches, useful flops, algorithmic operand bytes,
+      // problems), so that a profiler's per-launch DRAM bytes can be set against
+      // the work of that launch
+      static long long umma_launches = 0;
+      static FILE* umma_log = [] {
+        const char* p = getenv("QCA_UMMA_LOG");
+        return p && *p ? fopen(p, "w") : (FILE*)nullptr;
+      }();
+      if (umma_log) {
+        double f = 0.0, b = 0.0;
+        for (auto& d : big) {
+          const double nb = (double)d.nb1 * d.nb2 * d.G;
+          f += 8.0 * d.M * d.N * (double)d.K * nb;
+          b += sizeof(cplx<T>) *
+               ((double)d.M * d.K * nb + (double)d.K * d.N * nb + (double)d.M * d.N * d.nb1 * d.nb2);
+        }
+        fprintf(umma_log, "%lld %.0f %.0f %zu\n", umma_launches, f, b, big.size());
+        fflush(umma_log);
+      }
+      ++umma_launches;
+    }
     const GemmDesc<T>* db = nullptr;
     const GemmDesc<T>* ds = nullptr;
     if (!big.empty()) QCA_TRY(upload(big, st, &db));

@@ -123,10 +123,12 @@ def test_poisson_trace_shape():
     assert all(50 <= j.spec.steps <= 500 for j in jobs)
 
 
-def _fake_serving(monkeypatch):
+def _fake_serving(monkeypatch, fail=None):
     """The serving module with its engine faked on the host: every tick of every
     chain completes one local update; a chain completes a time step after
-    ``ticks_per_step`` ticks; every engine call takes one second of a fake clock."""
+    ``ticks_per_step`` ticks; every engine call takes one second of a fake clock.
+    ``fail`` maps a chain id to the tick at which that chain reports QCA_ERR_NAN."""
+    fail = fail or {}
     from qca_gb300 import serving
     clock = {"t": 0.0}
     chains = {}
@@ -149,9 +151,17 @@ def _fake_serving(monkeypatch):
             chains[args[1]]["todo"] += args[2]
         elif name == "qca_engine_advance":
             ids = [args[1][i] for i in range(args[2])]
+            failed = []
             for _ in range(args[3]):
                 for cid in ids:
                     c = chains[cid]
+                    if c.get("status"):
+                        continue
+                    c["ticks"] = c.get("ticks", 0) + 1
+                    if fail.get(cid) == c["ticks"]:
+                        c["status"] = serving._lib.QCA_ERR_NAN
+                        failed.append(cid)
+                        continue
                     if c["todo"] > 0:
                         c["tick"] += 1
                         if c["tick"] == ticks_per_step:
@@ -159,9 +169,15 @@ def _fake_serving(monkeypatch):
                             c["todo"] -= 1
                             c["done"] += 1
             clock["t"] += 1.0
+            if failed:
+                raise serving._lib.QcaError(serving._lib.QCA_ERR_NAN, f"chain {failed[0]}: non-finite values")
+        elif name == "qca_engine_step_chains":
+            c = chains[args[1][0]]
+            if c.get("status"):
+                raise serving._lib.QcaError(c["status"], f"chain {args[1][0]} failed in an earlier step (at tick {fail[args[1][0]]})")
         elif name == "qca_chain_progress":
             c = chains[args[1]]
-            args[2][0], args[2][1], args[2][2], args[2][3] = c["done"], c["todo"], int(c["tick"] > 0), 0
+            args[2][0], args[2][1], args[2][2], args[2][3] = c["done"], c["todo"], int(c["tick"] > 0), c.get("status", 0)
         elif name == "qca_chain_remove":
             del chains[args[1]]
     fake_call.next_id = 0
@@ -194,6 +210,25 @@ def test_serving_jobs_progress_at_their_own_pace(monkeypatch):
     assert srv.active[0].steps_done == 4 and len(srv.active[0].stream) == 1
     rep = srv.run([], time_limit=3.5)
     assert rep["elapsed_s"] <= 3.5 + 1.0 and rep["jobs_done"] == 2 and rep["jobs_active"] == 1
+
+
+def test_serving_retires_a_failed_job_with_the_engine_message(monkeypatch):
+    """A job whose chain fails numerically is retired with the engine's account of
+    the failure (status code and message) while the others complete; the report
+    counts it by status and lists it with its specification."""
+    from qca_gb300.workloads import ChainSpec
+    serving, clock, calls = _fake_serving(monkeypatch, fail={2: 4})
+    spec = ChainSpec(n=6, distance=1, interval=range(1, 2), chi=4, p=np.full(6, 0.5), steps=3)
+    srv = serving.Server("mixed", hbm_budget_bytes=1 << 30, stream_every=2, max_resident=4, ticks_per_round=5)
+    for _ in range(3):
+        srv.submit(spec, arrival=0.0)
+    rep = srv.run([], time_limit=None)
+    assert rep["jobs_done"] == 2 and rep["jobs_failed"] == 1
+    assert rep["failures_by_status"] == {str(serving._lib.QCA_ERR_NAN): 1}
+    assert "chain 2: non-finite values" in rep["first_failure"]
+    (f,) = rep["failed_jobs"]
+    assert f["job"] == 1 and f["n"] == 6 and f["chi"] == 4 and f["algorithm"] == "2tdvp"
+    assert "failed in an earlier step (at tick 4)" in f["error"]
 
 
 def test_bench_roofline_arithmetic():
