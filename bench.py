@@ -156,6 +156,16 @@ def kernel_stats(eng) -> dict:
                         "bytes": out[4 * c + 3]} for c in range(len(KCLASS))}
 
 
+# DRAM traffic of one tcgen05 GEMM launch against its algorithmic operand bytes, from
+# one ncu capture (--set full) of the 201st gemm_umma_grouped launch of
+# `bench.py --chains 16 --steps 1 --warmup 2 --no-e2e --no-cpu --acc-chains 0`
+# on a GB300, the launch's work from the QCA_UMMA_LOG line of the same command
+# (summary: profiles/gemm_umma_batched_16chains_mixed.md).  The operands are mostly
+# L2 hits, so DRAM traffic is a fraction of the operand bytes; applied to the GEMM
+# class's operand bytes per launch of the run at hand.
+GEMM_DRAM_SAMPLE = {"dram_bytes": 1029888.0, "operand_bytes": 3183664.0, "useful_flops": 58133504.0}
+
+
 def tdvp_roofline(ks: dict, pk: dict, steps: int, timed_ms: float) -> dict:
     """Roofline object of the TDVP workloads from the per-class kernel statistics.
 
@@ -172,9 +182,13 @@ def tdvp_roofline(ks: dict, pk: dict, steps: int, timed_ms: float) -> dict:
     total_ms = sum(x["ms"] for x in ks.values())
     step_tflops = sum(x["flops"] for x in ks.values()) / (timed_ms / 1e3) / 1e12 if timed_ms > 0 else 0.0
     peak_3x = pk["bf16_tflops"] / 2.0 / 3.0
+    per_launch = gemm["bytes"] / gemm["launches"] if gemm["launches"] > 0 else 0.0
+    ratio = GEMM_DRAM_SAMPLE["dram_bytes"] / GEMM_DRAM_SAMPLE["operand_bytes"]
     return {"kernel": "gemm", "dominant_class": dom, "bound": "tensor",
             "achieved": round(tflops, 3), "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
-            "frac": round(tflops / pk["bf16_tflops"], 5), "traffic": None,
+            "frac": round(tflops / pk["bf16_tflops"], 5), "traffic": round(ratio * per_launch),
+            "traffic_basis": "bytes per GEMM launch: operand bytes per launch of this run x the DRAM/operand "
+                             f"ratio {ratio:.3f} of one ncu-captured tcgen05 launch (16-chain case)",
             "peak_source": f"{pk['source']} bf16 dense", "measured_kernel": "gemm",
             "peak_3xtf32_derived": round(peak_3x, 1), "frac_of_3xtf32": round(tflops / peak_3x, 4),
             "step_algorithmic_tflops": round(step_tflops, 3),
@@ -715,6 +729,7 @@ def run_serving(args, dist: Dist):
         return {"site_updates_per_s": round(r["site_updates_per_s"], 1), "jobs_done": r["jobs_done"],
                 "jobs_failed": r["jobs_failed"], "failures_by_status": r["failures_by_status"],
                 "first_failure": r["first_failure"], "failed_jobs": r["failed_jobs"][:16],
+                "jobs_escalated": r["jobs_escalated"], "escalations_by_status": r["escalations_by_status"],
                 "jobs_unfinished": r["jobs_active"] + r["jobs_pending"],
                 "p50_latency_s": r["p50_latency_s"], "p99_latency_s": r["p99_latency_s"],
                 "p50_first_populations_s": r["p50_first_stream_s"],

@@ -1,4 +1,5 @@
 // Error capture and library-level entry points of the C ABI.
+#include <atomic>
 #include <cstdarg>
 
 #include "common.cuh"
@@ -7,7 +8,12 @@ namespace qca {
 
 namespace {
 thread_local char g_error[1024] = "";
+std::atomic<long long> g_launches{0};
 }
+
+void count_launches(int k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+
+long long launches_so_far() { return g_launches.load(std::memory_order_relaxed); }
 
 void set_error(const char* fmt, ...) {
   va_list ap;

@@ -19,6 +19,11 @@ namespace qca {
 void set_error(const char* fmt, ...);
 const char* last_error();
 
+// Kernels launched by the TDVP engine's launch functions (process-wide): the
+// engine's per-class statistics count kernels, not grouped-launch regions.
+void count_launches(int k);
+long long launches_so_far();
+
 #define QCA_CUDA(call)                                                                    \
   do {                                                                                    \
     cudaError_t _e = (call);                                                              \

@@ -252,7 +252,7 @@ struct Engine final : EngineBase {
   struct Pend {
     int cls;
     cudaEvent_t a, b;
-    double flops, bytes;
+    double flops, bytes, kernels;
   };
   std::vector<cudaEvent_t> ev_pool;
   size_t ev_used = 0;
@@ -271,17 +271,18 @@ struct Engine final : EngineBase {
   int timed(int cls, double flops, double bytes, cudaStream_t st, F&& f) {
     if (!prof) return f();
     cudaEvent_t a = next_event(), b = next_event();
+    const long long k0 = launches_so_far();
     cudaEventRecord(a, st);
     const int s = f();
     cudaEventRecord(b, st);
-    pend.push_back(Pend{cls, a, b, flops, bytes});
+    pend.push_back(Pend{cls, a, b, flops, bytes, (double)(launches_so_far() - k0)});
     return s;
   }
   void resolve() {
     for (auto& p : pend) {
       float ms = 0.f;
       cudaEventElapsedTime(&ms, p.a, p.b);
-      acc[p.cls][0] += 1;
+      acc[p.cls][0] += p.kernels;
       acc[p.cls][1] += ms;
       acc[p.cls][2] += p.flops;
       acc[p.cls][3] += p.bytes;

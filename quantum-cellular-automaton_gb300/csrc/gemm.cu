@@ -154,6 +154,7 @@ int launch_gemm(const GemmDesc<T>* d_desc, const GemmDesc<T>* h_desc, int ndesc,
       break;
   }
   QCA_LAUNCH_CHECK();
+  count_launches(1);
   return QCA_OK;
 }
 
@@ -385,6 +386,7 @@ int launch_gemm_tc(const GemmDesc<float>* d_desc, const GemmDesc<float>* h_desc,
   }
   gemm_tc_grouped<<<tiles, 256, 2 * sizeof(TcSmem), st>>>(d_desc, ndesc);
   QCA_LAUNCH_CHECK();
+  count_launches(1);
   return QCA_OK;
 }
 

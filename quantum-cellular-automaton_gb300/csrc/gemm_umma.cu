@@ -429,6 +429,7 @@ int launch_gemm_umma(const GemmDesc<float>* d_desc, const GemmDesc<float>* h_des
   const int grid = tiles < sms ? tiles : sms;
   gemm_umma_grouped<<<grid, kUmThreads, kUmSmem, st>>>(d_desc, ndesc, tiles);
   QCA_LAUNCH_CHECK();
+  count_launches(1);
   return QCA_OK;
 }
 

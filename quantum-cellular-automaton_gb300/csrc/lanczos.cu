@@ -6,7 +6,8 @@
 // tdvp.py:164-188).  Here v <- exp(-i tau H_eff) v is computed by Lanczos with
 // the basis resident on the device and classical Gram-Schmidt applied twice
 // (projections accumulated in FP64).  At the convergence check points (every
-// third iteration, on breakdown and at the iteration limit) one warp per problem
+// third iteration, at the iteration limit and when the Krylov space is exhausted:
+// m = n, or beta_j at the rounding level of ||H v_j||) one warp per problem
 // evaluates exp(-i tau T) e_1 of the tridiagonal T by a sub-stepped Taylor series
 // (FP64) and stops when beta_j |(exp(-i tau T) e_1)_j| < tol; in between it only
 // records beta_j.  A finished problem's later launches return at once (done flag).
@@ -19,6 +20,14 @@ namespace {
 constexpr int kLzThreads = 256;
 constexpr int kLzPer = kLzChunk / kLzThreads;  // elements per thread
 constexpr int kPartStride = kLzPartStride;
+
+// rounding level of the Lanczos recurrence relative to ||H v_j|| (vectors stored in
+// T, matrix-vector products accumulated over long sums): a beta_j below it is
+// indistinguishable from zero
+template <typename T>
+__device__ __forceinline__ double lz_noise() {
+  return sizeof(T) == 4 ? 64.0 * 1.2e-7 : 64.0 * 2.2e-16;
+}
 
 template <typename D>
 __device__ __forceinline__ int find_tile(const D* d, int nd, int tile) {
@@ -245,7 +254,16 @@ __global__ void lz_finalize_kernel(const LanczosDesc<T>* __restrict__ descs, int
   bsq = warp_sum(bsq);
   const double beta = sqrt(bsq);
   const int m = j + 1;  // T is m x m: alpha_0..alpha_j, beta_0..beta_{j-1}
-  if (!check && isfinite(beta) && beta >= S[LZ_TOL] * 1e-3 && m + 1 <= mmax && m + 1 <= kLzMax) {
+  // The Krylov space is exhausted when it spans the whole problem (m = n) or when
+  // beta_j falls to the rounding level of the recurrence w = H v_j - alpha_j v_j -
+  // beta_{j-1} v_{j-1}, whose terms are of size ||H v_j|| (this includes the energy
+  // of the rest of the chain carried by the environments, large on long chains):
+  // a vector normalised from that residue is rounding noise, not orthogonal to the
+  // basis, and continuing from it corrupts T.  T is then exact to working
+  // precision and the exponential is taken from it.
+  const double ja = S[LZ_ALPHA + j], jb = j > 0 ? S[LZ_BETA + j - 1] : 0.0;
+  const bool exhausted = (long long)m >= D.n || beta <= lz_noise<T>() * sqrt(ja * ja + jb * jb);
+  if (!check && !exhausted && isfinite(beta) && beta >= S[LZ_TOL] * 1e-3 && m + 1 <= mmax && m + 1 <= kLzMax) {
     // not a convergence check point: record beta_j and continue without the
     // tridiagonal exponential (evaluated at check points, breakdown and the end)
     if (lane == 0) {
@@ -349,8 +367,8 @@ __global__ void lz_finalize_kernel(const LanczosDesc<T>* __restrict__ descs, int
       S[LZ_FLAG] = 1.0;
       *done = 1;
       if (D.status) atomicOr(D.status, kLzStatusNonFinite);
-    } else if (err < tol || beta < 1e-300 || m + 1 > mmax || m + 1 > kLzMax) {
-      if (!(err < tol) && !(beta < 1e-300)) {
+    } else if (err < tol || beta < 1e-300 || exhausted || m + 1 > mmax || m + 1 > kLzMax) {
+      if (!(err < tol) && !(beta < 1e-300) && !exhausted) {
         S[LZ_FLAG] = 2.0;  // iteration limit reached
         if (D.status) atomicOr(D.status, kLzStatusLimit);
       }
@@ -469,6 +487,7 @@ int launch_wapply(const WapplyDesc<T>* d_desc, const WapplyDesc<T>* h_desc, int 
   if (tiles <= 0) return QCA_OK;
   wapply_kernel<T><<<tiles, 256, 0, st>>>(d_desc, nd);
   QCA_LAUNCH_CHECK();
+  count_launches(1);
   return QCA_OK;
 }
 
@@ -480,6 +499,8 @@ int launch_lz_init(const LanczosDesc<T>* d, const LanczosDesc<T>* h, int nd, int
   lz_norm_kernel<T><<<tiles, kLzThreads, 0, st>>>(d, nd);
   lz_init_kernel<T><<<tiles, kLzThreads, 0, st>>>(d, nd, tol);
   QCA_LAUNCH_CHECK();
+  count_launches(1);
+  count_launches(1);  // lz_norm_kernel
   return QCA_OK;
 }
 
@@ -488,6 +509,7 @@ int launch_lz_orth_pass(const LanczosDesc<T>* d, const LanczosDesc<T>* h, int nd
   const int tiles = h[nd - 1].tile_begin + h[nd - 1].chunks;
   lz_orth_kernel<T><<<tiles, kLzThreads, 0, st>>>(d, nd, j, pass);
   QCA_LAUNCH_CHECK();
+  count_launches(1);
   return QCA_OK;
 }
 
@@ -495,6 +517,7 @@ template <typename T>
 int launch_lz_finalize_j(const LanczosDesc<T>* d, int nd, int j, int mmax, int check, cudaStream_t st) {
   lz_finalize_kernel<T><<<nd, 32, 0, st>>>(d, nd, j, mmax, check);
   QCA_LAUNCH_CHECK();
+  count_launches(1);
   return QCA_OK;
 }
 
@@ -503,6 +526,7 @@ int launch_lz_normalize(const LanczosDesc<T>* d, const LanczosDesc<T>* h, int nd
   const int tiles = h[nd - 1].tile_begin + h[nd - 1].chunks;
   lz_normalize_kernel<T><<<tiles, kLzThreads, 0, st>>>(d, nd, j);
   QCA_LAUNCH_CHECK();
+  count_launches(1);
   return QCA_OK;
 }
 
@@ -512,6 +536,7 @@ int launch_lz_combine(const LanczosDesc<T>* d, const LanczosDesc<T>* h, int nd, 
   const int tiles = h[nd - 1].tile_begin + h[nd - 1].chunks;
   lz_combine_kernel<T><<<tiles, kLzThreads, 0, st>>>(d, nd);
   QCA_LAUNCH_CHECK();
+  count_launches(1);
   return QCA_OK;
 }
 
@@ -522,6 +547,7 @@ int launch_copy(const CopyDesc<T>* d, const CopyDesc<T>* h, int nd, cudaStream_t
   if (tiles <= 0) return QCA_OK;
   copy_kernel<T><<<tiles, 256, 0, st>>>(d, nd);
   QCA_LAUNCH_CHECK();
+  count_launches(1);
   return QCA_OK;
 }
 
@@ -530,6 +556,7 @@ int launch_rho(const RhoDesc<T>* d, int nd, cudaStream_t st) {
   if (nd <= 0) return QCA_OK;
   rho_kernel<T><<<nd, 256, 0, st>>>(d);
   QCA_LAUNCH_CHECK();
+  count_launches(1);
   return QCA_OK;
 }
 

@@ -177,6 +177,7 @@ int launch_qr(const QrDesc<T>* d, int nd, int gauge, cudaStream_t st) {
   else
     qr_kernel<T, double><<<nd, kQrThreads, 0, st>>>(d);
   QCA_LAUNCH_CHECK();
+  count_launches(1);
   return QCA_OK;
 }
 

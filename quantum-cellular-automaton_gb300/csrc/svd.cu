@@ -701,6 +701,7 @@ static int launch_clustered(void (*kern)(Args...), int ctas, int cs, size_t smem
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   QCA_CUDA(cudaLaunchKernelEx(&cfg, kern, args...));
+  count_launches(1);
   return QCA_OK;
 }
 

@@ -14,8 +14,10 @@ jobs join at any round (continuous batching at local-update granularity).
 <n_i> is streamed every ``stream_every`` steps and at the end of each job through
 ``on_populations(job_id, step, populations)`` on a completion thread, so user code
 that consumes the populations overlaps with the next round on the GPU.  A job
-that fails numerically (QCA_ERR_NAN / QCA_ERR_NOT_CONVERGED) is retired with its
-error and does not stop the others.
+that fails numerically (QCA_ERR_NAN / QCA_ERR_NOT_CONVERGED) does not stop the
+others; on the mixed-precision server it is restarted from its initial state on a
+plain FP64 engine (``escalate``, the default: mixed 1TDVP grown from product states
+on long chains is not robust), elsewhere it is retired with its error.
 
 This replaces the reference's per-state driver loop (``quantum_game.py:28-119``:
 one initial state at a time, measure every plot interval) with a multi-job
@@ -50,13 +52,20 @@ class JobState:
     bytes: int = 0
     error: str | None = None
     stream: list = field(default_factory=list)
+    engine: object = None     # the _Engine holding the job's chain
+    precision: int = 0
+    escalated: bool = False   # restarted on the FP64 engine after a mixed failure
 
 
 class Server:
     def __init__(self, precision: str = "mixed", hbm_budget_bytes: int = 150 << 30, stream_every: int = 10,
-                 max_resident: int = 512, on_populations=None, ticks_per_round: int = 32) -> None:
+                 max_resident: int = 512, on_populations=None, ticks_per_round: int = 32,
+                 escalate: bool = True) -> None:
         self.precision = _lib.QCA_PREC_MIXED if precision == "mixed" else _lib.QCA_PREC_FP64
         self.engine = _Engine(self.precision, hbm_budget_bytes)
+        self.escalate = escalate and self.precision == _lib.QCA_PREC_MIXED
+        self._fp64_engine = None                # created at the first escalation
+        self.escalations: dict[int, int] = {}   # status code -> jobs restarted in FP64
         self.budget = hbm_budget_bytes
         self.used = 0
         self.stream_every = stream_every
@@ -85,23 +94,26 @@ class Server:
         self.pending.append(js)
         return js.job_id
 
-    def footprint(self, spec: ChainSpec) -> int:
+    def footprint(self, spec: ChainSpec, precision: int | None = None) -> int:
         mps = spec.mps()
         d, keep = chain_desc(mps.A, spec.mpo().W, spec.algorithm, spec.dt, spec.chi, spec.eps)
         size = ctypes.c_size_t()
-        _lib.call("qca_chain_footprint", ctypes.byref(d), self.precision, ctypes.byref(size))
+        _lib.call("qca_chain_footprint", ctypes.byref(d), self.precision if precision is None else precision,
+                  ctypes.byref(size))
         return size.value
 
     def _schedule_next(self, js: JobState) -> None:
         target = min(js.spec.steps, js.steps_done + self.stream_every)
         if target > js.scheduled_to:
-            _lib.call("qca_chain_schedule", self.engine.h, js.chain, target - js.scheduled_to)
+            _lib.call("qca_chain_schedule", js.engine.h, js.chain, target - js.scheduled_to)
             js.scheduled_to = target
 
     def _admit(self, now: float) -> None:
         while self.pending and self.pending[0].arrival <= now and len(self.active) < self.max_resident:
             js = self.pending[0]
-            need = self.footprint(js.spec)
+            if js.engine is None:
+                js.engine, js.precision = self.engine, self.precision
+            need = self.footprint(js.spec, js.precision)
             if need > self.budget:
                 raise _lib.AdmissionError(_lib.QCA_ERR_ADMISSION, f"job {js.job_id} needs {need} bytes > budget")
             if self.used + need > self.budget:
@@ -110,7 +122,7 @@ class Server:
             mps = js.spec.mps()
             d, keep = chain_desc(mps.A, js.spec.mpo().W, js.spec.algorithm, js.spec.dt, js.spec.chi, js.spec.eps)
             cid = ctypes.c_int(-1)
-            _lib.call("qca_chain_add", self.engine.h, ctypes.byref(d), None, ctypes.byref(cid))
+            _lib.call("qca_chain_add", js.engine.h, ctypes.byref(d), None, ctypes.byref(cid))
             js.chain = cid.value
             js.bytes = need
             js.admitted = now
@@ -120,7 +132,7 @@ class Server:
 
     def _progress(self, js: JobState) -> tuple[int, bool, int]:
         pr = (ctypes.c_longlong * 4)()
-        _lib.call("qca_chain_progress", self.engine.h, js.chain, pr)
+        _lib.call("qca_chain_progress", js.engine.h, js.chain, pr)
         return int(pr[0]), bool(pr[2]), int(pr[3])
 
     def _failure_message(self, js: JobState, status: int) -> str:
@@ -128,19 +140,42 @@ class Server:
         step request on a failed chain returns its recorded error without running."""
         ids = (ctypes.c_int * 1)(js.chain)
         try:
-            _lib.call("qca_engine_step_chains", self.engine.h, ids, 1, 1, None)
+            _lib.call("qca_engine_step_chains", js.engine.h, ids, 1, 1, None)
         except _lib.QcaError as e:
             return str(e)
         return f"status {status}"
 
+    def _groups(self, jobs: list[JobState]) -> list[list[JobState]]:
+        """Jobs by the engine that holds them (one grouped call per engine)."""
+        g: dict[int, list[JobState]] = {}
+        for j in jobs:
+            g.setdefault(id(j.engine), []).append(j)
+        return list(g.values())
+
+    def _escalate(self, js: JobState, status: int) -> None:
+        """Restart a job that failed on the mixed engine from its initial state on
+        the FP64 engine; it keeps its arrival time (latency counts from there)."""
+        _lib.call("qca_chain_remove", js.engine.h, js.chain)
+        self.used -= js.bytes
+        self.site_updates -= js.steps_done * js.spec.site_updates_per_step()  # redone in FP64
+        self.escalations[status] = self.escalations.get(status, 0) + 1
+        if self._fp64_engine is None:
+            self._fp64_engine = _Engine(_lib.QCA_PREC_FP64, self.budget)
+        js.engine, js.precision, js.escalated = self._fp64_engine, _lib.QCA_PREC_FP64, True
+        js.chain, js.bytes, js.steps_done, js.scheduled_to = -1, 0, 0, 0
+        js.stream = []
+        self.pending.appendleft(js)
+
     def _measure(self, jobs: list[JobState]) -> None:
-        if not jobs:
-            return
+        for group in self._groups(jobs):
+            self._measure_group(group)
+
+    def _measure_group(self, jobs: list[JobState]) -> None:
         ids = (ctypes.c_int * len(jobs))(*[j.chain for j in jobs])
         n_tot = sum(j.spec.n for j in jobs)
         pop = np.zeros(n_tot)
-        _lib.call("qca_engine_measure", self.engine.h, ids, len(jobs), pop.ctypes.data_as(_lib._PD), None, None,
-                  None, None)
+        _lib.call("qca_engine_measure", jobs[0].engine.h, ids, len(jobs), pop.ctypes.data_as(_lib._PD), None,
+                  None, None, None)
         o = 0
         for j in jobs:
             p = pop[o:o + j.spec.n].copy()
@@ -151,7 +186,7 @@ class Server:
 
     def _retire(self, js: JobState, t: float, failed: bool = False) -> None:
         js.finished = t
-        _lib.call("qca_chain_remove", self.engine.h, js.chain)
+        _lib.call("qca_chain_remove", js.engine.h, js.chain)
         self.used -= js.bytes
         (self.failed if failed else self.done).append(js)
 
@@ -167,21 +202,25 @@ class Server:
         if not self.active:
             return bool(self.pending)
         self.max_overlap = max(self.max_overlap, len(self.active))
-        ids = (ctypes.c_int * len(self.active))(*[j.chain for j in self.active])
-        try:
-            _lib.call("qca_engine_advance", self.engine.h, ids, len(self.active),
-                      self.ticks_per_round if ticks is None else ticks, None)
-        except _lib.QcaError as e:
-            if e.code not in (_lib.QCA_ERR_NAN, _lib.QCA_ERR_NOT_CONVERGED):
-                raise
-            if self.first_failure is None:
-                self.first_failure = str(e)
+        for group in self._groups(self.active):
+            ids = (ctypes.c_int * len(group))(*[j.chain for j in group])
+            try:
+                _lib.call("qca_engine_advance", group[0].engine.h, ids, len(group),
+                          self.ticks_per_round if ticks is None else ticks, None)
+            except _lib.QcaError as e:
+                if e.code not in (_lib.QCA_ERR_NAN, _lib.QCA_ERR_NOT_CONVERGED):
+                    raise
+                if self.first_failure is None:
+                    self.first_failure = str(e)
         due, still = [], []
         t = time.perf_counter()
         for j in self.active:
             done, inside, status = self._progress(j)
             if status:
                 j.error = self._failure_message(j, status)
+                if self.escalate and not j.escalated:
+                    self._escalate(j, status)
+                    continue
                 self.failures[status] = self.failures.get(status, 0) + 1
                 self._retire(j, t, failed=True)
                 continue
@@ -260,6 +299,8 @@ class Server:
         return {"jobs_done": len(self.done), "jobs_failed": len(self.failed),
                 "failures_by_status": {str(k): v for k, v in self.failures.items()},
                 "first_failure": self.first_failure,
+                "jobs_escalated": sum(self.escalations.values()),
+                "escalations_by_status": {str(k): v for k, v in self.escalations.items()},
                 "failed_jobs": [{"job": j.job_id, "algorithm": j.spec.algorithm, "n": j.spec.n,
                                  "distance": j.spec.distance, "chi": j.spec.chi, "steps_done": j.steps_done,
                                  "error": j.error} for j in self.failed],

@@ -219,16 +219,46 @@ def test_serving_retires_a_failed_job_with_the_engine_message(monkeypatch):
     from qca_gb300.workloads import ChainSpec
     serving, clock, calls = _fake_serving(monkeypatch, fail={2: 4})
     spec = ChainSpec(n=6, distance=1, interval=range(1, 2), chi=4, p=np.full(6, 0.5), steps=3)
-    srv = serving.Server("mixed", hbm_budget_bytes=1 << 30, stream_every=2, max_resident=4, ticks_per_round=5)
+    srv = serving.Server("mixed", hbm_budget_bytes=1 << 30, stream_every=2, max_resident=4, ticks_per_round=5,
+                         escalate=False)
     for _ in range(3):
         srv.submit(spec, arrival=0.0)
     rep = srv.run([], time_limit=None)
-    assert rep["jobs_done"] == 2 and rep["jobs_failed"] == 1
+    assert rep["jobs_done"] == 2 and rep["jobs_failed"] == 1 and rep["jobs_escalated"] == 0
     assert rep["failures_by_status"] == {str(serving._lib.QCA_ERR_NAN): 1}
     assert "chain 2: non-finite values" in rep["first_failure"]
     (f,) = rep["failed_jobs"]
     assert f["job"] == 1 and f["n"] == 6 and f["chi"] == 4 and f["algorithm"] == "2tdvp"
     assert "failed in an earlier step (at tick 4)" in f["error"]
+
+
+def test_serving_restarts_a_failed_mixed_job_in_fp64(monkeypatch):
+    """On the mixed-precision server a job whose chain fails numerically is restarted
+    from its initial state on an FP64 engine (a second engine, created then), keeps
+    its arrival time, and completes; the site updates of its failed attempt are not
+    counted; the report counts the escalation by status."""
+    from qca_gb300.workloads import ChainSpec
+    serving, clock, calls = _fake_serving(monkeypatch, fail={2: 4})
+    engines = []
+    base = serving._Engine
+
+    class Recording(base):
+        def __init__(self, *a, **k):
+            super().__init__(*a, **k)
+            engines.append(a[0] if a else None)
+
+    monkeypatch.setattr(serving, "_Engine", Recording)
+    spec = ChainSpec(n=6, distance=1, interval=range(1, 2), chi=4, p=np.full(6, 0.5), steps=3)
+    srv = serving.Server("mixed", hbm_budget_bytes=1 << 30, stream_every=2, max_resident=4, ticks_per_round=5)
+    for _ in range(3):
+        srv.submit(spec, arrival=0.0)
+    rep = srv.run([], time_limit=None)
+    assert rep["jobs_done"] == 3 and rep["jobs_failed"] == 0
+    assert rep["jobs_escalated"] == 1 and rep["escalations_by_status"] == {str(serving._lib.QCA_ERR_NAN): 1}
+    assert engines == [serving._lib.QCA_PREC_MIXED, serving._lib.QCA_PREC_FP64]
+    (j,) = [j for j in srv.done if j.escalated]
+    assert j.job_id == 1 and j.arrival == 0.0 and j.precision == serving._lib.QCA_PREC_FP64
+    assert rep["site_updates"] == 3 * 3 * spec.site_updates_per_step()
 
 
 def test_bench_roofline_arithmetic():

@@ -190,3 +190,28 @@ def test_oracle_a1tdvp_matches_reference(golden, name):
         assert np.array_equal(bonds, t[name + "_ref_bonds"][s]), s
         if s < steps:
             orc.step()
+
+
+def test_1tdvp_growth_from_product_states_is_ill_conditioned():
+    """Characterises the reference algorithm, not an implementation: 1TDVP grows its
+    bonds from the complement columns of complete QRs of rank-deficient site
+    matrices (tdvp.py:65-105), and those columns are set by rounding-level residues,
+    so a 1e-14 perturbation of the initial product state moves the populations
+    after one step by orders of magnitude more (5.6e-7 at N = 20, about 1.5e-5 at
+    N = 88), while 2TDVP passes it through at its own size.  This bounds how closely
+    any two implementations of 1TDVP can agree on long chains."""
+    n = 20
+    p = np.sin(O.random_thetas(n, 5)) ** 2
+    W = O.build_mpo(O.Rules(n, range(1, 2), 2))
+    rng = np.random.default_rng(1)
+
+    def run(alg, pert):
+        A = O.mps_from_density_distribution(p)
+        if pert:
+            A = [a + pert * (rng.standard_normal(a.shape) + 1j * rng.standard_normal(a.shape)) for a in A]
+        orc = O.TDVPKrylovOracle(A, W, alg, 0.05, 16, 1e-10)
+        orc.step()
+        return orc.measure()[0]
+
+    assert np.abs(run("1tdvp", 0.0) - run("1tdvp", 1e-14)).max() > 1e-8
+    assert np.abs(run("2tdvp", 0.0) - run("2tdvp", 1e-14)).max() < 1e-12

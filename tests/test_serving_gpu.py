@@ -80,3 +80,23 @@ def test_failed_job_is_retired_and_the_others_complete():
         alone.round(now=1e9)
     got = {j.job_id: j for j in srv.done}[1].stream
     assert np.abs(got[-1][1] - alone.done[0].stream[-1][1]).max() < 1e-12
+
+
+def test_mixed_failure_is_restarted_in_fp64():
+    """On the mixed-precision server a job that fails numerically is restarted on an
+    FP64 engine; a job that fails there too (a NaN in its initial state) is retired,
+    and the other jobs complete in mixed precision."""
+    from qca_gb300 import _lib
+    from qca_gb300.serving import Server
+    ss = specs()[:3]
+    bad = specs()[2]
+    bad.p = bad.p.copy()
+    bad.p[3] = np.nan
+    srv = Server("mixed", hbm_budget_bytes=8 << 30, stream_every=5)
+    for s in ss + [bad]:
+        srv.submit(s, 0.0)
+    while srv.pending or srv.active:
+        srv.round(now=1e9)
+    assert len(srv.done) == 3 and all(not j.escalated for j in srv.done)
+    assert len(srv.failed) == 1 and srv.failed[0].job_id == 3 and srv.failed[0].escalated
+    assert srv.escalations == {_lib.QCA_ERR_NAN: 1} and srv.failures == {_lib.QCA_ERR_NAN: 1}
