@@ -51,8 +51,15 @@ __global__ void __launch_bounds__(kQrThreads) qr_kernel(const QrDesc<T>* __restr
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int k = 0; k < K; ++k) {
     cplx<T>* col = A + (long long)k * m;
+    // squares in FP64: an FP32 square underflows below |x| ~ 1e-22, and the residue
+    // columns of rank-deficient matrices (1TDVP's complete QRs) reach that range;
+    // an underflowed norm makes beta come from alpha alone, v = x / (alpha - beta)
+    // huge and the reflector far from unitary
     double xs = 0.0;
-    for (int i = k + 1 + threadIdx.x; i < m; i += blockDim.x) xs += (double)norm2(col[i]);
+    for (int i = k + 1 + threadIdx.x; i < m; i += blockDim.x) {
+      const cplx<T> x = col[i];
+      xs += (double)x.re * (double)x.re + (double)x.im * (double)x.im;
+    }
     xs = block_sum(xs, red);
     const cplx<T> al = col[k];
     const double ar = al.re, ai = al.im;

@@ -178,30 +178,20 @@ def test_tdvp_mixed_tracks_fp64_at_large_bonds(alg_name):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_1tdvp_long_chain(precision):
-    """1TDVP on an 88-site chain (bond cap 16), one step from a product state.
+    """1TDVP on an 88-site chain (bond cap 16), one step from a product state,
+    completes in both precisions within 2e-4 of the Krylov oracle.
 
-    FP64: completes, and the populations stay within 2e-4 of the Krylov oracle.
-    That bound is set by the algorithm, not the precision: 1TDVP's complement
-    columns amplify rounding (a 1e-14 perturbation of the initial state moves the
-    oracle's own populations by 1.5e-5 after one step at this size; measured GPU
-    FP64 deviation 3-6e-5).
-
-    Mixed: known limitation.  On chains beyond about 50 sites the first left sweep
-    meets effective Hamiltonians with absurd Rayleigh quotients (cause not found; not
-    the tensor-core GEMMs, a build with CUDA-core FP32 GEMMs fails alike), and the
-    engine reports it: the step either completes within the same bound or raises
-    QCA_ERR_NAN / QCA_ERR_NOT_CONVERGED naming the chain -- never a silent result.
-    The serving loop restarts such jobs in FP64."""
-    from qca_gb300 import _lib
+    The bound is set by the algorithm, not the precision: 1TDVP's complement columns
+    amplify rounding (a 1e-14 perturbation of the initial state moves the oracle's
+    own populations by 1.5e-5 after one step at this size; measured GPU FP64
+    deviation 3-6e-5).  The mixed case is the regression test of the Householder
+    norm: with its squares taken in FP32 the residue columns of the rank-deficient
+    complete QRs underflowed, the reflectors lost unitarity and the first left sweep
+    failed with QCA_ERR_NAN."""
     n, chi = 88, 16
     p = np.sin(O.random_thetas(n, 5)) ** 2
     alg = make("1tdvp", n, 2, 1, 2, p, 0.05, chi, 1e-10, precision)
-    try:
-        alg.evolve(1)
-    except _lib.QcaError as e:
-        assert precision == "mixed", str(e)
-        assert e.code in (_lib.QCA_ERR_NAN, _lib.QCA_ERR_NOT_CONVERGED) and "chain" in str(e)
-        return
+    alg.evolve(1)
     r = rows(n)
     alg.measure(*r)
     assert np.all(np.isfinite(r[0]))
