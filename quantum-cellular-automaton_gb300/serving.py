@@ -16,8 +16,8 @@ jobs join at any round (continuous batching at local-update granularity).
 that consumes the populations overlaps with the next round on the GPU.  A job
 that fails numerically (QCA_ERR_NAN / QCA_ERR_NOT_CONVERGED) does not stop the
 others; on the mixed-precision server it is restarted from its initial state on a
-plain FP64 engine (``escalate``, the default: mixed 1TDVP grown from product states
-on long chains is not robust), elsewhere it is retired with its error.
+plain FP64 engine (``escalate``, the default), elsewhere it is retired with its
+error.
 
 This replaces the reference's per-state driver loop (``quantum_game.py:28-119``:
 one initial state at a time, measure every plot interval) with a multi-job
