@@ -1,5 +1,5 @@
 """Exact state-vector path on the GPU against the oracle and the reference's
-own outputs.  Tolerances: max|d<n_i>| <= 1e-10 for the FP64 path (north-star
+own outputs.  Tolerances: max|d<n_i>| <= 1e-10 for the FP64 path (the target
 bound for exact), <= 1e-5 for the mixed (complex64) path."""
 import types
 

@@ -1,7 +1,7 @@
 """TDVP on the GPU against the reference's own outputs (gauge-consistent form,
 golden fixtures from tests/golden/make_golden.py) and against the oracle.
 
-Tolerances (spec bounds): FP64 plain path max|d<n_i>| <= 1e-8 with
+Tolerances (the target bounds): FP64 plain path max|d<n_i>| <= 1e-8 with
 identical truncated bond dimensions; mixed path max|d<n_i>| <= 1e-5 for 2TDVP.
 Mixed 1TDVP is held to 5e-5: its bond growth uses the complement columns of a
 complete QR (tdvp.py:74, 95) of nearly rank-deficient matrices, and below the
