@@ -191,7 +191,7 @@ int qca_chain_stats_ex(qca_engine* e, int chain_id, double* stats, int count);
 /* Profiling hook (no counterpart in the reference, which has no tracing): when
  * enabled, every grouped launch is bracketed by CUDA events on its stream.
  * qca_engine_kernel_stats writes 7 kernel classes x 4 values
- * (launches, milliseconds, algorithmic real flops, algorithmic bytes); classes:
+ * (kernels launched, milliseconds, algorithmic real flops, algorithmic bytes); classes:
  * 0 GEMM contractions, 1 sparse MPO application, 2 Lanczos vector kernels,
  * 3 Lanczos tridiagonal exponential, 4 SVD, 5 QR, 6 other. */
 int qca_engine_profile(qca_engine* e, int enable);
