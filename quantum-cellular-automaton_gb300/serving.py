@@ -55,17 +55,25 @@ class JobState:
     engine: object = None     # the _Engine holding the job's chain
     precision: int = 0
     escalated: bool = False   # restarted on the FP64 engine after a mixed failure
+    cost: float = 0.0         # relative cost of one local update (chi^3 w, x2 for two-site)
 
 
 class Server:
     def __init__(self, precision: str = "mixed", hbm_budget_bytes: int = 150 << 30, stream_every: int = 10,
                  max_resident: int = 512, on_populations=None, ticks_per_round: int = 32,
-                 escalate: bool = True) -> None:
+                 escalate: bool = True, light_share: int = 4, light_ratio: float = 8.0) -> None:
         self.precision = _lib.QCA_PREC_MIXED if precision == "mixed" else _lib.QCA_PREC_FP64
         self.engine = _Engine(self.precision, hbm_budget_bytes)
         self.escalate = escalate and self.precision == _lib.QCA_PREC_MIXED
         self._fp64_engine = None                # created at the first escalation
         self.escalations: dict[int, int] = {}   # status code -> jobs restarted in FP64
+        # Lock-step ticks last as long as the costliest resident local update, so a
+        # job whose updates cost at most 1/light_ratio of the costliest one gets
+        # light_share times the ticks of a round (the extra ticks in a call of their
+        # own, short because no large job takes part); a job's arithmetic does not
+        # depend on how its ticks are grouped.
+        self.light_share = max(1, light_share)
+        self.light_ratio = light_ratio
         self.budget = hbm_budget_bytes
         self.used = 0
         self.stream_every = stream_every
@@ -120,7 +128,10 @@ class Server:
                 break  # wait for memory to free up
             self.pending.popleft()
             mps = js.spec.mps()
-            d, keep = chain_desc(mps.A, js.spec.mpo().W, js.spec.algorithm, js.spec.dt, js.spec.chi, js.spec.eps)
+            W = js.spec.mpo().W
+            d, keep = chain_desc(mps.A, W, js.spec.algorithm, js.spec.dt, js.spec.chi, js.spec.eps)
+            w = max(max(int(x.shape[2]), int(x.shape[3])) for x in W)  # MPO bonds: W[s, s', wl, wr]
+            js.cost = float(js.spec.chi) ** 3 * w * (2.0 if js.spec.algorithm == "2tdvp" else 1.0)
             cid = ctypes.c_int(-1)
             _lib.call("qca_chain_add", js.engine.h, ctypes.byref(d), None, ctypes.byref(cid))
             js.chain = cid.value
@@ -191,6 +202,18 @@ class Server:
         (self.failed if failed else self.done).append(js)
 
     # ------------------------------------------------------------------ loop
+    def _advance(self, group: list[JobState], ticks: int) -> None:
+        """Up to ``ticks`` lock-step ticks over one engine's jobs; a numerical failure
+        is recorded here and acted on from the jobs' progress."""
+        ids = (ctypes.c_int * len(group))(*[j.chain for j in group])
+        try:
+            _lib.call("qca_engine_advance", group[0].engine.h, ids, len(group), ticks, None)
+        except _lib.QcaError as e:
+            if e.code not in (_lib.QCA_ERR_NAN, _lib.QCA_ERR_NOT_CONVERGED):
+                raise
+            if self.first_failure is None:
+                self.first_failure = str(e)
+
     def round(self, now: float | None = None, ticks: int | None = None) -> bool:
         """Admit what has arrived, run up to ``ticks`` lock-step ticks over the
         resident jobs, stream the populations of jobs that reached their next
@@ -202,16 +225,14 @@ class Server:
         if not self.active:
             return bool(self.pending)
         self.max_overlap = max(self.max_overlap, len(self.active))
+        nt = self.ticks_per_round if ticks is None else ticks
         for group in self._groups(self.active):
-            ids = (ctypes.c_int * len(group))(*[j.chain for j in group])
-            try:
-                _lib.call("qca_engine_advance", group[0].engine.h, ids, len(group),
-                          self.ticks_per_round if ticks is None else ticks, None)
-            except _lib.QcaError as e:
-                if e.code not in (_lib.QCA_ERR_NAN, _lib.QCA_ERR_NOT_CONVERGED):
-                    raise
-                if self.first_failure is None:
-                    self.first_failure = str(e)
+            self._advance(group, nt)
+        if self.light_share > 1:
+            top = max(j.cost for j in self.active)
+            light = [j for j in self.active if j.cost * self.light_ratio <= top]
+            for group in self._groups(light):
+                self._advance(group, (self.light_share - 1) * nt)
         due, still = [], []
         t = time.perf_counter()
         for j in self.active:

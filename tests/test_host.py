@@ -261,6 +261,39 @@ def test_serving_restarts_a_failed_mixed_job_in_fp64(monkeypatch):
     assert rep["site_updates"] == 3 * 3 * spec.site_updates_per_step()
 
 
+@pytest.mark.parametrize("share", [1, 4])
+def test_serving_light_jobs_take_extra_ticks(monkeypatch, share):
+    """A job whose local updates cost far less than the costliest resident job's
+    (chi 4 against chi 64) gets ``light_share`` times the ticks of a round, in a
+    call of its own (the heavy job's chain is not in it), and finishes in fewer
+    rounds; with a share of 1 both progress alike."""
+    from qca_gb300.workloads import ChainSpec
+    serving, clock, calls = _fake_serving(monkeypatch)
+    advanced = []
+    real = serving._lib.call
+
+    def spy(name, *args):
+        if name == "qca_engine_advance":
+            advanced.append(([args[1][i] for i in range(args[2])], args[3]))
+        return real(name, *args)
+
+    monkeypatch.setattr(serving._lib, "call", spy)
+    heavy = ChainSpec(n=6, distance=1, interval=range(1, 2), chi=64, p=np.full(6, 0.5), steps=3)
+    light = ChainSpec(n=6, distance=1, interval=range(1, 2), chi=4, p=np.full(6, 0.5), steps=3)
+    srv = serving.Server("mixed", hbm_budget_bytes=1 << 30, stream_every=10, max_resident=4, ticks_per_round=3,
+                         light_share=share)
+    srv.submit(heavy, arrival=0.0)
+    srv.submit(light, arrival=0.0)
+    srv.round(now=0.0)  # 3 ticks = 1 step for both; the light job gets 3 (share - 1) more ticks
+    if share == 1:
+        assert advanced == [([1, 2], 3)] and srv.done == []
+    else:
+        assert advanced == [([1, 2], 3), ([2], 9)]
+        assert [j.job_id for j in srv.done] == [1] and srv.active[0].job_id == 0
+    rep = srv.run([], time_limit=None)
+    assert rep["jobs_done"] == 2
+
+
 def test_bench_roofline_arithmetic():
     """bench.py's roofline object from per-class kernel statistics (the numbers of
     a recorded batched run): the GEMM class against the measured bf16 peak, the
