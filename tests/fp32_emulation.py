@@ -9,7 +9,9 @@ Lanczos local exponentials) with
   (FP32 accumulation), Krylov projections in FP64, tolerance 1e-7 as on the device,
 * optionally, a Hermitian error of a given size in the Gram matrix of every
   split's isometric factor: U -> U (I + E / 2), U^H U = I + E + O(E^2), which is
-  what a one-sided Jacobi stopped at a rotation tolerance leaves behind.
+  what a one-sided Jacobi stopped at a rotation tolerance leaves behind,
+* optionally, one Newton-Schulz polar step in complex64 that restores the
+  isometry after the split (the correction proposed for the device).
 
 The splits themselves are the oracle's FP64 SVDs; everything else follows
 ``algorithms/tdvp.py`` through the oracle.
@@ -64,8 +66,9 @@ class FP32KrylovOracle(O.TDVPKrylovOracle):
     """The Krylov oracle with the mixed path's FP32 storage and products, and an
     optional isometry error of size ``isometry_error`` in every split."""
 
-    def __init__(self, *args, isometry_error: float = 0.0, seed: int = 0, **kw) -> None:
+    def __init__(self, *args, isometry_error: float = 0.0, seed: int = 0, polar: bool = False, **kw) -> None:
         self.isometry_error = isometry_error
+        self.polar = polar
         self._rng = np.random.default_rng(seed)
         self._right = True
         super().__init__(*args, **kw)
@@ -87,17 +90,40 @@ class FP32KrylovOracle(O.TDVPKrylovOracle):
             self.R[site] = e.astype(np.complex128)
 
     def _split(self, Al, Ar, L, R, Wl, Wr):
+        """The oracle's split, then the device's arithmetic around it: the isometric
+        factor U carries a Gram error (U -> U (I + E/2)), the other factor is formed
+        from that U as on the device (U^H Theta, i.e. (I + E/2) times the exact one),
+        and optionally both are corrected by one Newton-Schulz step
+        M = (3I - U^H U) / 2: U <- U M, other <- M other."""
         a, sk, b = super()._split(Al, Ar, L, R, Wl, Wr)
+        k = len(sk)
+        if not self.isometry_error and not self.polar:
+            return r32(a), sk, r32(b)
+        c = np.complex64
+        E = np.zeros((k, k))
         if self.isometry_error:
-            k = len(sk)
-            E = self._rng.uniform(-1, 1, (k, k)) + 1j * self._rng.uniform(-1, 1, (k, k))
-            G = np.eye(k) + (E + E.conj().T) / 4 * self.isometry_error
-            if self._right:  # the left factor is the isometry of a right-moving split
-                s = a.shape
-                a = (a.reshape(-1, k) @ G).reshape(s)
-            else:
-                s = b.shape
-                b = (G @ b.transpose(1, 0, 2).reshape(k, -1)).reshape(k, s[0], s[2]).transpose(1, 0, 2)
+            R_ = self._rng.uniform(-1, 1, (k, k)) + 1j * self._rng.uniform(-1, 1, (k, k))
+            E = (R_ + R_.conj().T) / 2 * self.isometry_error
+        P = np.eye(k) + E / 2
+        sa, sb = a.shape, b.shape
+        if self._right:  # U = a (rows (s, l)), other = diag(sk) b (rows k)
+            U = r32(a.reshape(-1, k) @ P)
+            X = r32(P @ (sk[:, None] * b.transpose(1, 0, 2).reshape(k, -1)))
+            if self.polar:
+                U32 = U.astype(c)
+                M = (3 * np.eye(k, dtype=c) - U32.conj().T @ U32) / 2
+                U, X = r32(U32 @ M), r32(M @ X.astype(c))
+            a = U.reshape(sa)
+            b = (X / sk[:, None]).reshape(k, sb[0], sb[2]).transpose(1, 0, 2)
+        else:  # U = b (rows k), other = a diag(sk)
+            B = r32(P @ b.transpose(1, 0, 2).reshape(k, -1))
+            Y = r32((a.reshape(-1, k) * sk[None, :]) @ P)
+            if self.polar:
+                B32 = B.astype(c)
+                M = (3 * np.eye(k, dtype=c) - B32 @ B32.conj().T) / 2
+                B, Y = r32(M @ B32), r32(Y.astype(c) @ M)
+            b = B.reshape(k, sb[0], sb[2]).transpose(1, 0, 2)
+            a = (Y / sk[None, :]).reshape(sa)
         return r32(a), sk, r32(b)
 
     def _sweep_right_2(self):
