@@ -326,6 +326,26 @@ class RefSampler:
     def rate(self) -> float:
         return self.done / self.used if self.used > 0 else 0.0
 
+    def predicted_rate_at_caps(self) -> float:
+        """Site-updates/s the reference algorithm would reach on the whole workload
+        with every bond at its cap min(2^i, 2^(N-i), chi), from the cost model
+        a + c n^3 calibrated in this run: per 2TDVP time step each bond is one
+        two-site update (dense problem n = 4 D_l D_r) and each inner site one
+        backward single-site update (n = 2 D_l D_r).  A model, not a measurement:
+        at chi = 128 one two-site update is a dense 65536^3 eigendecomposition."""
+        t = 0.0
+        su = 0
+        for sp in self.specs:
+            n = sp.n
+            D = [min(2 ** min(i, 40), 2 ** min(n - i, 40), sp.chi) for i in range(n + 1)]
+            for _ in range(2):  # right and left sweep
+                for l in range(n - 1):
+                    t += self.predict(4 * D[l] * D[l + 2])
+                for s_ in range(1, n - 1):
+                    t += self.predict(2 * D[s_] * D[s_ + 1])
+            su += sp.site_updates_per_step()
+        return su / t if t > 0 else 0.0
+
     def describe(self) -> str:
         return (f"{self.done} local updates of the reference algorithm (oracle restatement of tdvp.py: dense "
                 f"effective Hamiltonian + eigh) in {self.used:.1f} s, evolving chains 0..{self.ci} of the workload "
@@ -339,7 +359,8 @@ def cpu_tdvp_sample(specs, budget_s: float):
     over a bounded sample of the workload (``RefSampler``)."""
     rs = RefSampler(specs, per_update_limit_s=min(5.0, budget_s / 3))
     rs.sample(budget_s)
-    return rs.rate(), rs.describe()
+    return rs.rate(), rs.describe() + (f"; cost model a + c n^3 at every bond's cap: "
+                                       f"{rs.predicted_rate_at_caps():.3g} site-updates/s")
 
 
 def run_tdvp(args, dist: Dist):
@@ -628,7 +649,8 @@ def run_reference(args, dist: Dist):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": desc},
             "cpu_baseline": {"value": round(v, 3), "unit": "site-updates/s", "cores": os.cpu_count(), "kind": "port",
-                             "sample": rs.describe()},
+                             "sample": rs.describe(),
+                             "model_rate_at_bond_caps": float(f"{rs.predicted_rate_at_caps():.3g}")},
             "e2e": {"value": round(v, 3), "unit": "site-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
