@@ -498,8 +498,11 @@ def accuracy_leg(args, specs, pops_batched, batched_value: float) -> dict:
         del eng
     done = len(series["fp64"])
     dn = np.abs(series["mixed"][:done] - series["fp64"]).max(axis=1)
+    within = [bool(x <= 1e-5) for x in dn]
     return {"max_dn_vs_fp64": float(dn.max()), "max_dn_by_step": [float(f"{x:.3g}") for x in dn],
             "steps_compared": done, "steps_run_mixed": total, "chains": len(specs),
+            "bound": 1e-5, "within_bound_all_steps": all(within),
+            "steps_within_bound_from_start": next((i for i, w in enumerate(within) if not w), len(within)),
             "chains_desc": [(s.n, s.distance, s.interval.stop - 1, s.chi) for s in specs],
             "batched_vs_alone_max_dn": float(np.abs(series["mixed"][-1] - pops_batched).max()),
             "fp64": {"site_updates_per_s": round(rates["fp64"], 2),
