@@ -55,6 +55,7 @@ class JobState:
     engine: object = None     # the _Engine holding the job's chain
     precision: int = 0
     escalated: bool = False   # restarted on the FP64 engine after a mixed failure
+    mixed_error: str | None = None  # the engine's message of that mixed failure
     cost: float = 0.0         # relative cost of one local update (chi^3 w, x2 for two-site)
 
 
@@ -173,6 +174,7 @@ class Server:
         if self._fp64_engine is None:
             self._fp64_engine = _Engine(_lib.QCA_PREC_FP64, self.budget)
         js.engine, js.precision, js.escalated = self._fp64_engine, _lib.QCA_PREC_FP64, True
+        js.mixed_error, js.error = js.error, None
         js.chain, js.bytes, js.steps_done, js.scheduled_to = -1, 0, 0, 0
         js.stream = []
         self.pending.appendleft(js)

@@ -258,6 +258,7 @@ def test_serving_restarts_a_failed_mixed_job_in_fp64(monkeypatch):
     assert engines == [serving._lib.QCA_PREC_MIXED, serving._lib.QCA_PREC_FP64]
     (j,) = [j for j in srv.done if j.escalated]
     assert j.job_id == 1 and j.arrival == 0.0 and j.precision == serving._lib.QCA_PREC_FP64
+    assert j.error is None and "failed in an earlier step" in j.mixed_error
     assert rep["site_updates"] == 3 * 3 * spec.site_updates_per_step()
 
 
