@@ -402,3 +402,25 @@ def test_batched_workload_definition():
     assert all(np.array_equal(x.p, y.p) for x, y in zip(a, b))
     assert [(s.n, s.chi) for s in a] != [(s.n, s.chi) for s in c]
     assert sum(s.site_updates_per_step() for s in a) == sum(2 * (s.n - 1) for s in a)
+
+
+def test_reference_sampler_is_bounded_and_models_the_caps():
+    """bench.py's reference arm: a sample never runs past its budget by more than
+    one update, counts the local updates it ran, and its cost model at the bond
+    caps falls as the caps grow (dense n^3 problems)."""
+    import sys
+    import time
+    sys.path.insert(0, ROOT)
+    import bench
+    from qca_gb300 import workloads as W
+    specs = W.chain_mix(4, seed=1000, n_lo=8, n_hi=12, chis=(8, 16))
+    rs = bench.RefSampler(specs, per_update_limit_s=1.0)
+    t0 = time.perf_counter()
+    done, used = rs.sample(1.5)
+    assert done > 0 and used <= 1.5 + 1.0 and time.perf_counter() - t0 < 10.0
+    assert rs.rate() > 0
+    caps = rs.predicted_rate_at_caps()
+    assert caps > 0
+    rs16 = bench.RefSampler([W.ChainSpec(s.n, s.distance, s.interval, 64, s.p) for s in specs], 1.0)
+    rs16.c, rs16.a = rs.c, rs.a
+    assert rs16.predicted_rate_at_caps() < caps
